@@ -1,0 +1,148 @@
+/*
+ * spd_gb300 -- C ABI of the GB300 (sm_103a) SD-ADER step for the
+ * compressible Euler equations.
+ *
+ * The reference (jpalafou/spd) has no foreign-function layer: its operator
+ * interface is the Python class SDADER_Simulator
+ * (src/sdader_simulator.py:14).  Each entry point below replaces one method
+ * of that class; the Python package spd_gb300 binds them with ctypes and
+ * keeps the class surface.  All arrays crossing this boundary are host
+ * FP64 arrays in the reference's C-order layouts:
+ *
+ *   U_sp, U_cv, W_cv   (V, Nz, Ny, Nx, nz, ny, nx)          SD layout
+ *   troubles           (1, Z, Y, X)                         Z = Nz*(p+1) ...
+ *   theta              (1, Z+4, Y+4, X+4)
+ *   affected_faces_x   (1, Z, Y, X+1)   (_y: (1, Z, Y+1, X), _z: (1, Z+1, Y, X))
+ *   BC_fp_<dim>        (2, V, m+1, other cells..., other points...)
+ *   BC_fv_<dim>        (2, V, extended extents with 2 along <dim>)
+ *
+ * with absent dimensions dropped (1D: (V, Nx, nx); 2D: (V, Ny, Nx, ny, nx)).
+ * V = ndim + 2 variables ordered (rho, v_x[, v_y[, v_z]], P or E).
+ *
+ * Every function returns 0 on success and a nonzero spd_status otherwise;
+ * spd_last_error() gives the message.  A context owns one CUDA stream and
+ * its device buffers; it is not thread-safe, separate contexts may be used
+ * from separate threads.  There is no CPU fallback: spd_create fails when
+ * no CUDA device is available.
+ */
+#ifndef SPD_GB300_H
+#define SPD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct spd_ctx spd_ctx;
+
+enum spd_status {
+  SPD_OK = 0,
+  SPD_ERR_ARG = 1,      /* invalid argument or unsupported option */
+  SPD_ERR_CUDA = 2,     /* CUDA runtime error */
+  SPD_ERR_NONFINITE = 3 /* dt is not finite */
+};
+
+enum spd_riemann { SPD_LLF = 0, SPD_HLLC = 1, SPD_LHLLC = 2 };
+enum spd_limiter { SPD_MINMOD = 0, SPD_MONCEN = 1 };
+enum spd_update { SPD_UPDATE_SD = 0, SPD_UPDATE_FV = 1 };
+enum spd_bc {
+  SPD_BC_PERIODIC = 0,
+  SPD_BC_REFLECTIVE = 1,
+  SPD_BC_GRADFREE = 2,
+  SPD_BC_IC = 3,
+  SPD_BC_EQ = 4,
+  SPD_BC_PRESSURE = 5
+};
+
+enum spd_field {
+  SPD_U_SP = 0,
+  SPD_U_CV = 1,
+  SPD_W_CV = 2,
+  SPD_TROUBLES = 3,
+  SPD_THETA = 4,
+  SPD_AFFECTED_X = 5,
+  SPD_AFFECTED_Y = 6,
+  SPD_AFFECTED_Z = 7,
+  SPD_BC_FP_X = 8,
+  SPD_BC_FP_Y = 9,
+  SPD_BC_FP_Z = 10,
+  SPD_BC_FV_X = 11,
+  SPD_BC_FV_Y = 12,
+  SPD_BC_FV_Z = 13
+};
+
+/* Constructor options of SDADER_Simulator (src/simulator.py:10-36,
+ * src/sd_simulator.py:20-26, src/fv_simulator.py:11-17,
+ * src/sdader_simulator.py:15-27).  Strings become the enums above. */
+typedef struct spd_config {
+  int ndim;              /* 1, 2 or 3 */
+  int N[3];              /* cells per direction, x first */
+  int p;                 /* polynomial degree, 1..4 */
+  int m;                 /* time order (m+1 ADER nodes), 0..5 */
+  double lim[3][2];      /* xlim, ylim, zlim */
+  double gamma;
+  double cfl_coeff;
+  double min_c2;
+  int riemann_solver_sd; /* spd_riemann */
+  int riemann_solver_fv; /* spd_riemann */
+  int slope_limiter;     /* spd_limiter */
+  int update;            /* spd_update */
+  int FB;
+  double tolerance;
+  int SED;
+  int NAD_delta;         /* NAD == "delta" */
+  int PAD;
+  int blending;
+  double min_rho, max_rho, min_P;
+  int godunov;
+  int BC[3][2];          /* spd_bc per direction and side */
+} spd_config;
+
+/* Constant operators built at setup on the host
+ * (src/sd_simulator.py:30-52, src/sdader_simulator.py:40-46,61-92),
+ * row-major. */
+typedef struct spd_operators {
+  const double* sp_to_fp;      /* (p+2) x (p+1) */
+  const double* dfp_to_sp;     /* (p+1) x (p+2) */
+  const double* sp_to_cv;      /* (p+1) x (p+1) */
+  const double* cv_to_sp;      /* (p+1) x (p+1) */
+  const double* invader;       /* (m+1) x (m+1), already weighted by w_tp */
+  const double* w_tp;          /* m+1 */
+  const double* faces[3];      /* subcell face positions with 2 ghost layers:
+                                  N*(p+1) + 5 values per direction */
+} spd_operators;
+
+/* SDADER_Simulator.__init__ (device part): allocate the context. */
+int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out);
+/* Copy a host array in the reference layout into the context. */
+int spd_upload(spd_ctx* ctx, int field, const double* host, size_t count);
+/* Copy a context array into a host buffer in the reference layout. */
+int spd_download(spd_ctx* ctx, int field, double* host, size_t count);
+/* SD_Simulator.compute_dt (src/sd_simulator.py:214-227). */
+int spd_compute_dt(spd_ctx* ctx, double* dt_out);
+/* Assign dm.dt (src/sdader_simulator.py:408). */
+int spd_set_dt(spd_ctx* ctx, double dt);
+int spd_get_dt(spd_ctx* ctx, double* dt_out);
+/* SDADER_Simulator.perform_update (src/sdader_simulator.py:361-378) with
+ * the current dt; *time_inout += dt on return. */
+int spd_perform_update(spd_ctx* ctx, double* time_inout);
+/* The loop bodies of perform_iterations (:394-399) and
+ * perform_time_evolution (:401-413), without init_sim / end_sim.
+ * mode 0: n_step iterations of (compute_dt, perform_update);
+ * mode 1: advance while *time_inout < t_end with the t_end clip and the
+ *         dt < 1e-14 stop.  *nsteps_done receives the steps taken. */
+int spd_step(spd_ctx* ctx, int nsteps, double t_end, int mode, double* time_inout, int* nsteps_done);
+/* SDADER_Simulator.end_sim (:385-392): U_cv = sp_to_cv(U_sp), W_cv = prim(U_cv). */
+int spd_end_sim(spd_ctx* ctx);
+/* Wait for all work of the context. */
+int spd_synchronize(spd_ctx* ctx);
+int spd_destroy(spd_ctx* ctx);
+const char* spd_last_error(const spd_ctx* ctx);
+const char* spd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPD_GB300_H */

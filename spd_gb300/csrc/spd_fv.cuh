@@ -1,0 +1,600 @@
+// Subcell finite-volume update with a-posteriori limiting for sm_103a:
+// high-order flux application, ghost fills, NAD/SED/PAD trouble detection,
+// blending, MUSCL-Hancock fallback fluxes on the affected faces only, and
+// the CFL reduction.  Bit-identical to src/sdader_simulator.py:333-349,
+// src/fv_simulator.py, src/trouble_detection.py and src/muscl.py.
+#pragma once
+#include "spd_kernels.cuh"
+
+namespace spd {
+
+struct FvGeo {
+  const double* dx[3];       // active subcell widths, X_d values
+  const double* centers[3];  // extended subcell centres, Xe_d values
+  const double* hfp[3];      // extended subcell widths, Xe_d values
+  const double* hcv[3];      // extended centre distances, Xe_d - 1 values
+};
+
+__device__ __forceinline__ void q_coords(const Geo& g, long long q, int& ix, int& iy, int& iz) {
+  ix = (int)(q % g.X[0]);
+  long long r = q / g.X[0];
+  iy = (int)(r % g.X[1]);
+  iz = (int)(r / g.X[1]);
+}
+
+template <int D>
+__device__ __forceinline__ long long ext_of(const Geo& g, int ix, int iy, int iz) {
+  const int xe = ix + NGH, ye = (D >= 2) ? iy + NGH : 0, ze = (D >= 3) ? iz + NGH : 0;
+  return xe + (long long)g.Xe[0] * (ye + (long long)g.Xe[1] * ze);
+}
+
+__device__ __forceinline__ long long ext_stride(const Geo& g, int d) {
+  return d == 0 ? 1LL : (d == 1 ? (long long)g.Xe[0] : (long long)g.Xe[0] * g.Xe[1]);
+}
+
+__device__ __forceinline__ long long face_id(const Geo& g, int d, int fx, int fy, int fz) {
+  const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
+  return fx + (long long)FX * (fy + (long long)FY * fz);
+}
+
+__host__ __device__ __forceinline__ long long n_faces(const Geo& g, int d) {
+  return (long long)(g.X[0] + (d == 0)) * (g.X[1] + (d == 1)) * (g.X[2] + (d == 2));
+}
+
+// dUdt of one subcell from the face fluxes (src/fv_simulator.py:189-205)
+template <int D>
+__device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, int ix, int iy, int iz,
+                                                const double* const* F, int v, double& out) {
+  const int ii[3] = {ix, iy, iz};
+  double acc = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const long long nf = n_faces(g, d);
+    const long long fl = face_id(g, d, ix, iy, iz);
+    const long long fr = face_id(g, d, ix + (d == 0), iy + (d == 1), iz + (d == 2));
+    const double part = (F[d][(long long)v * nf + fr] - F[d][(long long)v * nf + fl]) / fg.dx[d][ii[d]];
+    acc = (d == 0) ? part : acc + part;
+  }
+  out = acc;
+}
+
+// candidate update with the high-order fluxes of time node i, W_old and
+// W_new into the extended arrays (src/sdader_simulator.py:336-340,
+// src/trouble_detection.py:10-13)
+template <int D>
+__global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i,
+                               const double* F0, const double* F1, const double* F2,
+                               const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
+                               double* ext_new, int write_ext) {
+  constexpr int V = D + 2;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= g.Nq) return;
+  int ix, iy, iz;
+  q_coords(g, q, ix, iy, iz);
+  const double* F[3] = {F0, F1, F2};
+  const double dti = *dt_ptr * w_i;
+  double u[V], un[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    double dudt;
+    flux_divergence<D>(g, fg, ix, iy, iz, F, v, dudt);
+    un[v] = u[v] - dudt * dti;
+    U_new[(long long)v * g.Nq + q] = un[v];
+  }
+  if (write_ext) {
+    const long long e = ext_of<D>(g, ix, iy, iz);
+    double W[V];
+    prim<D>(u, W, g.gamma, 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) ext_old[(long long)v * g.Nqe + e] = W[v];
+    prim<D>(un, W, g.gamma, 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
+  }
+}
+
+// ghost fill of one direction (src/fv_simulator.py:224-273): store the
+// boundary buffer when the reference does, then copy it into the ghost
+// layers.  bcbuf layout [side][v][g][other], other = the extended index of
+// the remaining directions (lower direction fastest).  When ``gate`` is
+// non-null the fill runs only if *gate != 0.
+template <int D>
+__global__ void k_ghost(Geo g, int d, int all, int nv, int nv_buf, double* ext, double* bcbuf, const int* gate) {
+  if (gate != nullptr && *gate == 0) return;
+  const int o0 = (d == 0) ? 1 : 0;
+  const int o1 = (d == 2) ? 1 : 2;
+  const long long nother = (long long)g.Xe[o0] * g.Xe[o1];
+  const long long total = 2LL * nv * NGH * nother;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= total) return;
+  const long long other = tid % nother;
+  long long r = tid / nother;
+  const int gi = (int)(r % NGH);
+  r /= NGH;
+  const int v = (int)(r % nv);
+  const int side = (int)(r / nv);
+  const int a = (int)(other % g.Xe[o0]);
+  const int b = (int)(other / g.Xe[o0]);
+  const int Xd = g.X[d];
+  const int kind = g.bc[d][side];
+  auto ext_index = [&](int e) -> long long {
+    int c[3];
+    c[d] = e;
+    c[o0] = a;
+    c[o1] = b;
+    return c[0] + (long long)g.Xe[0] * (c[1] + (long long)g.Xe[1] * c[2]);
+  };
+  const long long bidx = (((long long)side * nv_buf + v) * NGH + gi) * nother + other;
+  double val;
+  bool store = false;
+  int src = 0;
+  if (kind == BC_PERIODIC) { store = true; src = (side == 0) ? Xd + gi : NGH + gi; }
+  else if ((kind == BC_REFLECTIVE || kind == BC_GRADFREE) && all) { store = true; src = (side == 0) ? NGH + gi : Xd + gi; }
+  if (store) {
+    val = ext[(long long)v * g.Nqe + ext_index(src)];
+    if (kind == BC_REFLECTIVE && v == d + 1) val = val * -1.0;
+    bcbuf[bidx] = val;
+  } else if (kind == BC_EQ && all) {
+    val = 0.0;
+    bcbuf[bidx] = val;
+  } else {
+    val = bcbuf[bidx];
+  }
+  const int dst = (side == 0) ? gi : Xd + NGH + gi;
+  ext[(long long)v * g.Nqe + ext_index(dst)] = val;
+}
+
+// NAD: relaxed discrete maximum principle over the cross stencil
+// (src/trouble_detection.py:14-38).  mask bit v = possible trouble of var v.
+template <int D>
+__global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __restrict__ ext_old,
+                      const double* __restrict__ ext_new, unsigned char* __restrict__ mask, int* any_flag) {
+  constexpr int V = D + 2;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int m = 0;
+  if (q < g.Nq) {
+    int ix, iy, iz;
+    q_coords(g, q, ix, iy, iz);
+    const long long e = ext_of<D>(g, ix, iy, iz);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const double* W = ext_old + (long long)v * g.Nqe;
+      const double c0 = W[e];
+      double mx = c0, mn = c0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const long long st = ext_stride(g, d);
+        const double a = W[e - st], b = W[e + st];
+        mx = np_max(np_max(a, b), mx);
+        mn = np_min(np_min(a, b), mn);
+      }
+      if (relax) {
+        if (delta) {
+          const double eps = tol * (mx - mn);
+          mn = mn - eps;
+          mx = mx + eps;
+        } else {
+          mn = mn - fabs(mn) * tol;
+          mx = mx + fabs(mx) * tol;
+        }
+      }
+      const double wn = ext_new[(long long)v * g.Nqe + e];
+      const bool pt = !(wn >= mn) || !(wn <= mx);
+      m |= (pt ? 1u : 0u) << v;
+    }
+    mask[q] = (unsigned char)m;
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, m != 0);
+  if (ballot != 0 && (threadIdx.x & 31) == 0) atomicOr(any_flag, 1);
+}
+
+// smooth-extrema relaxation factor of one variable along direction d at
+// active subcell i (src/trouble_detection.py:104-137, including its
+// one-sided minimum at the first and last active subcell).
+__device__ __forceinline__ double sed_alpha_dir(const double* W, long long e0, long long st, int i, int Xd,
+                                                const double* cen, const double* hfp) {
+  // line accessors in extended coordinates k along d
+  auto U = [&](int k) { return W[e0 + (long long)k * st]; };
+  auto dU = [&](int k) { return (U(k + 1) - U(k - 1)) / (cen[k + 1] - cen[k - 1]); };
+  auto aLR = [&](int k, double& aL, double& aR) {
+    const double dUm = dU(k - 1), dU0 = dU(k), dUp = dU(k + 1);
+    const double d2U = (dUp - dUm) / (cen[k + 1] - cen[k - 1]);
+    const double dv = 0.5 * hfp[k] * d2U;
+    const double vL = dUm - dU0;
+    const double vR = dUp - dU0;
+    const double selL = (dv < 0) ? ((vL > 0) ? vL : 0.0) : ((vL < 0) ? vL : 0.0);
+    aL = -selL / dv;
+    if (fabs(dv) <= 0.0) aL = 1.0;
+    aL = (aL < 1.0) ? aL : 1.0;
+    const double selR = (dv > 0) ? ((vR > 0) ? vR : 0.0) : ((vR < 0) ? vR : 0.0);
+    aR = selR / dv;
+    if (fabs(dv) <= 0.0) aR = 1.0;
+    aR = (aR < 1.0) ? aR : 1.0;
+  };
+  auto A = [&](int k) {
+    double aL, aR;
+    aLR(k, aL, aR);
+    return (aR < aL) ? aR : aL;
+  };
+  const int k = i + NGH;
+  if (i == 0) return np_min(A(k), A(k + 1));
+  if (i == Xd - 1) {
+    double aL, aR;
+    aLR(k, aL, aR);
+    return np_min(A(k - 1), aL);
+  }
+  return np_min(A(k - 1), np_min(A(k), A(k + 1)));
+}
+
+// SED + trouble flags + PAD (src/trouble_detection.py:40-70); writes the
+// troubles into var 0 of the theta-source extended array and the troubles
+// array.
+template <int D>
+__global__ void k_troubles(Geo g, FvGeo fg, int sed_enabled, int pad, double min_rho, double max_rho, double min_P,
+                           const unsigned char* __restrict__ mask, const int* __restrict__ any_flag,
+                           const double* __restrict__ ext_new, double* __restrict__ theta_src,
+                           double* __restrict__ troubles) {
+  constexpr int P_ = D + 1;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= g.Nq) return;
+  int ix, iy, iz;
+  q_coords(g, q, ix, iy, iz);
+  const long long e = ext_of<D>(g, ix, iy, iz);
+  const unsigned m = mask[q];
+  int pt0 = m & 1u, ptP = (m >> P_) & 1u;
+  if (sed_enabled && *any_flag && (pt0 || ptP)) {
+    const int ii[3] = {ix, iy, iz};
+    const int vars[2] = {0, P_};
+    int* pts[2] = {&pt0, &ptP};
+    for (int w = 0; w < 2; ++w) {
+      if (!*pts[w]) continue;
+      const double* W = ext_new + (long long)vars[w] * g.Nqe;
+      double alpha = W[e] * 0.0 + 1.0;
+      for (int d = 0; d < D; ++d) {
+        const long long st = ext_stride(g, d);
+        const long long e0 = e - (long long)(ii[d] + NGH) * st;
+        const double an = sed_alpha_dir(W, e0, st, ii[d], g.X[d], fg.centers[d], fg.hfp[d]);
+        alpha = (an < alpha) ? an : alpha;
+      }
+      *pts[w] = (alpha < 1.0) ? *pts[w] : 0;
+    }
+  }
+  double t = (pt0 > ptP) ? (double)pt0 : (double)ptP;
+  if (pad) {
+    const double r = ext_new[e];
+    const double P = ext_new[(long long)P_ * g.Nqe + e];
+    t = (r >= min_rho) ? t : 1.0;
+    t = (r <= max_rho) ? t : 1.0;
+    t = (P >= min_P) ? t : 1.0;
+  }
+  theta_src[e] = t;
+  troubles[q] = t;
+}
+
+// extended-grid coordinates
+__device__ __forceinline__ void e_coords(const Geo& g, long long e, int& xe, int& ye, int& ze) {
+  xe = (int)(e % g.Xe[0]);
+  long long r = e / g.Xe[0];
+  ye = (int)(r % g.Xe[1]);
+  ze = (int)(r / g.Xe[1]);
+}
+
+// first / second (/ third) neighbour blending (src/trouble_detection.py:
+// 139-164); the 3D neighbour pairs are those the reference's index tuples
+// select.
+template <int D>
+__global__ void k_blend_neighbours(Geo g, const double* __restrict__ src, double* __restrict__ out) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= g.Nqe) return;
+  int c[3];
+  e_coords(g, e, c[0], c[1], c[2]);
+  auto at = [&](int x, int y, int z) { return src[x + (long long)g.Xe[0] * (y + (long long)g.Xe[1] * z)]; };
+  auto inb = [&](int d, int v) { return v >= 0 && v < g.Xe[d]; };
+  double th = src[e];
+  for (int d = 0; d < D; ++d) {
+    for (int s = -1; s <= 1; s += 2) {
+      int cc[3] = {c[0], c[1], c[2]};
+      cc[d] += s;
+      if (inb(d, cc[d])) th = np_max(0.75 * at(cc[0], cc[1], cc[2]), th);
+    }
+  }
+  if (D == 2) {
+    for (int sy = -1; sy <= 1; sy += 2)
+      for (int sx = -1; sx <= 1; sx += 2)
+        if (inb(0, c[0] + sx) && inb(1, c[1] + sy)) th = np_max(0.5 * at(c[0] + sx, c[1] + sy, 0), th);
+  } else if (D == 3) {
+    // (axis pair, offsets) per (i, idim); axes listed as (first, second)
+    // cut axis; offset 0 with range e < last (cut a) or e >= 1 (cut b)
+    const int axes[3][2] = {{1, 0}, {2, 1}, {0, 2}};  // idim 0: (y,x); 1: (z,y); 2: (x,z)
+    // per i: (offset, cutkind) for the first and the second cut axis;
+    // cutkind 0 = a (target e < last), 1 = b (target e >= 1)
+    const int offs[4][2] = {{+1, +1}, {0, -1}, {-1, +1}, {0, -1}};
+    const int kinds[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};
+    for (int i = 0; i < 4; ++i) {
+      for (int idim = 0; idim < 3; ++idim) {
+        bool ok = true;
+        int cc[3] = {c[0], c[1], c[2]};
+        for (int k2 = 0; k2 < 2; ++k2) {
+          const int ax = axes[idim][k2];
+          const int last = g.Xe[ax] - 1;
+          if (kinds[i][k2] == 0 && c[ax] >= last) ok = false;
+          if (kinds[i][k2] == 1 && c[ax] < 1) ok = false;
+          cc[ax] += offs[i][k2];
+        }
+        if (ok) th = np_max(0.5 * at(cc[0], cc[1], cc[2]), th);
+      }
+    }
+    // third neighbours: offsets on (z, y, x)
+    const int t3[4][3] = {{+1, +1, +1}, {+1, +1, -1}, {+1, -1, +1}, {+1, -1, -1}};
+    for (int i = 0; i < 4; ++i) {
+      const int oz = t3[i][0], oy = t3[i][1], ox = t3[i][2];
+      const bool ok = (oz > 0 ? c[2] < g.Xe[2] - 1 : c[2] >= 1) && (oy > 0 ? c[1] < g.Xe[1] - 1 : c[1] >= 1) &&
+                      (ox > 0 ? c[0] < g.Xe[0] - 1 : c[0] >= 1);
+      if (ok) th = np_max(0.375 * at(c[0] + ox, c[1] + oy, c[2] + oz), th);
+    }
+  }
+  out[e] = th;
+}
+
+// last blending layer along direction d (src/trouble_detection.py:167-169):
+// two sequential in-place sweeps, fused with a one-cell halo.
+template <int D>
+__global__ void k_blend_last(Geo g, int d, const double* __restrict__ in, double* __restrict__ out) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= g.Nqe) return;
+  int c[3];
+  e_coords(g, e, c[0], c[1], c[2]);
+  const long long st = ext_stride(g, d);
+  const int last = g.Xe[d] - 1;
+  auto th_a = [&](int k, long long ek) {  // after the first sweep
+    const double t = in[ek];
+    if (k < last) return np_max(0.25 * ((in[ek + st] > 0) ? 1.0 : 0.0), t);
+    return t;
+  };
+  const int k = c[d];
+  const double a0 = th_a(k, e);
+  if (k >= 1) {
+    const double am = th_a(k - 1, e - st);
+    out[e] = np_max(0.25 * ((am > 0) ? 1.0 : 0.0), a0);
+  } else {
+    out[e] = a0;
+  }
+}
+
+// affected faces of direction d (src/trouble_detection.py:81-87) and the
+// marks for the fallback fluxes and the corrected update.
+template <int D>
+__global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__ theta, double* __restrict__ aff,
+                           unsigned char* __restrict__ mark_cell, unsigned char* __restrict__ mark_q,
+                           int* __restrict__ nmarked) {
+  const long long nf = n_faces(g, d);
+  const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool need = false;
+  if (fidx < nf) {
+    const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
+    int f[3];
+    f[0] = (int)(fidx % FX);
+    long long r = fidx / FX;
+    f[1] = (int)(r % FY);
+    f[2] = (int)(r / FY);
+    int e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+      const int base = (k < D) ? f[k] + NGH : 0;
+      e1[k] = base;
+      e2[k] = base;
+    }
+    e1[d] = f[d] + 1;
+    e2[d] = f[d] + 2;
+    const long long i1 = e1[0] + (long long)g.Xe[0] * (e1[1] + (long long)g.Xe[1] * e1[2]);
+    const long long i2 = e2[0] + (long long)g.Xe[0] * (e2[1] + (long long)g.Xe[1] * e2[2]);
+    const double a = np_max(theta[i1], theta[i2]);
+    aff[fidx] = a;
+    need = godunov || (a != 0.0);
+    if (need) {
+      mark_cell[i1] = 1;
+      mark_cell[i2] = 1;
+      int q[3] = {f[0], f[1], f[2]};
+      if (f[d] >= 1) {
+        q[d] = f[d] - 1;
+        mark_q[q[0] + (long long)g.X[0] * (q[1] + (long long)g.X[1] * q[2])] = 1;
+      }
+      if (f[d] < g.X[d]) {
+        q[d] = f[d];
+        mark_q[q[0] + (long long)g.X[0] * (q[1] + (long long)g.X[1] * q[2])] = 1;
+      }
+    }
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, need);
+  if (b != 0 && (threadIdx.x & 31) == 0) atomicAdd(nmarked, __popc(b));
+}
+
+// compaction of marked indices by warp ballot: writes the marked indices
+// into list and their count into *count.
+__global__ void k_compact(long long total, const unsigned char* __restrict__ mark, long long* __restrict__ list,
+                          unsigned long long* __restrict__ count) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool m = (i < total) && mark[i];
+  const unsigned b = __ballot_sync(0xffffffffu, m);
+  if (b == 0) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (m) list[base + __popc(b & ((1u << lane) - 1u))] = i;
+}
+
+// MUSCL-Hancock: limited gradients, slopes and the half-step primitive
+// predictor of one extended subcell (src/muscl.py:61-75,129-173,175-216).
+template <int D>
+__global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __restrict__ dt_ptr, double w_i,
+                              const long long* __restrict__ list, const unsigned long long* __restrict__ count,
+                              const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S) {
+  constexpr int V = D + 2, P_ = D + 1;
+  const unsigned long long cnt = *count;
+  const double dti = *dt_ptr * w_i;
+  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)gridDim.x * blockDim.x) {
+  const long long e = list[idx];
+  int c[3];
+  e_coords(g, e, c[0], c[1], c[2]);
+  double W[V], dMh[3][V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) W[v] = W_ext[(long long)v * g.Nqe + e];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const long long st = ext_stride(g, d);
+    const int k = c[d];
+    const double hl = fg.hcv[d][k - 1], hr = fg.hcv[d][k], hm = fg.hfp[d][k];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const double* M = W_ext + (long long)v * g.Nqe;
+      const double SL = (M[e] - M[e - st]) / hl;
+      const double SR = (M[e + st] - M[e]) / hr;
+      const double dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
+      dMh[d][v] = dm;
+      S[((long long)d * V + v) * g.Nqe + e] = 0.5 * dm * hm;
+    }
+  }
+  double dtW[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) dtW[v] = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int vel = d + 1;
+    const double* dW = dMh[d];
+    dtW[0] = dtW[0] - (W[vel] * dW[0] + W[0] * dW[vel]);
+    dtW[P_] = dtW[P_] - (W[vel] * dW[P_] + g.gamma * W[P_] * dW[vel]);
+    dtW[vel] = dtW[vel] - (W[vel] * dW[vel] + dW[P_] / W[0]);
+#pragma unroll
+    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - W[vel] * dW[v2];
+  }
+  dtW[P_] = dtW[P_] * 0.0;
+#pragma unroll
+  for (int v = 0; v < V; ++v) Mpred[(long long)v * g.Nqe + e] = W[v] + 0.5 * dtW[v] * dti;
+  }
+}
+
+// fallback Riemann flux on the affected faces of direction d
+// (src/muscl.py:217-221, src/fv_simulator.py:88-165)
+template <int D>
+__global__ void k_muscl_faces(Geo g, int d, int solver, int godunov, const double* __restrict__ aff,
+                              const double* __restrict__ Mpred, const double* __restrict__ S,
+                              double* __restrict__ F_FB) {
+  constexpr int V = D + 2;
+  const long long nf = n_faces(g, d);
+  const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (fidx >= nf) return;
+  const double a = aff[fidx];
+  if (!(godunov || a != 0.0)) return;
+  const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
+  int f[3];
+  f[0] = (int)(fidx % FX);
+  long long r = fidx / FX;
+  f[1] = (int)(r % FY);
+  f[2] = (int)(r / FY);
+  int e1[3];
+  for (int k = 0; k < 3; ++k) e1[k] = (k < D) ? f[k] + NGH : 0;
+  e1[d] = f[d] + 1;
+  const long long i1 = e1[0] + (long long)g.Xe[0] * (e1[1] + (long long)g.Xe[1] * e1[2]);
+  const long long i2 = i1 + ext_stride(g, d);
+  double ML[V], MR[V], F[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    ML[v] = Mpred[(long long)v * g.Nqe + i1] + S[((long long)d * V + v) * g.Nqe + i1];
+    MR[v] = Mpred[(long long)v * g.Nqe + i2] - S[((long long)d * V + v) * g.Nqe + i2];
+  }
+  riemann<D>(solver, ML, MR, F, g.gamma, g.min_c2, d, true);
+#pragma unroll
+  for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = F[v];
+}
+
+// corrected update of the subcells next to an affected face
+// (src/sdader_simulator.py:325-331,346)
+template <int D>
+__global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i, int godunov,
+                             const long long* __restrict__ list, const unsigned long long* __restrict__ count,
+                             const double* F0, const double* F1, const double* F2, const double* B0,
+                             const double* B1, const double* B2, const double* A0, const double* A1,
+                             const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new) {
+  constexpr int V = D + 2;
+  const unsigned long long cnt = *count;
+  const double* FH[3] = {F0, F1, F2};
+  const double* FB[3] = {B0, B1, B2};
+  const double* AF[3] = {A0, A1, A2};
+  const double dti = *dt_ptr * w_i;
+  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)gridDim.x * blockDim.x) {
+  const long long q = list[idx];
+  int ix, iy, iz;
+  q_coords(g, q, ix, iy, iz);
+  const int ii[3] = {ix, iy, iz};
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    double acc = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const long long nf = n_faces(g, d);
+      const long long fl = face_id(g, d, ix, iy, iz);
+      const long long fr = face_id(g, d, ix + (d == 0), iy + (d == 1), iz + (d == 2));
+      double Fv[2];
+      const long long fs[2] = {fl, fr};
+      for (int s = 0; s < 2; ++s) {
+        const double ho = FH[d][(long long)v * nf + fs[s]];
+        const double a = AF[d][fs[s]];
+        if (godunov) Fv[s] = 1.0 * FB[d][(long long)v * nf + fs[s]] + (1.0 - 1.0) * ho;
+        else if (a != 0.0) Fv[s] = a * FB[d][(long long)v * nf + fs[s]] + (1.0 - a) * ho;
+        else Fv[s] = ho;
+      }
+      const double part = (Fv[1] - Fv[0]) / fg.dx[d][ii[d]];
+      acc = (d == 0) ? part : acc + part;
+    }
+    U_new[(long long)v * g.Nq + q] = U_cv[(long long)v * g.Nq + q] - acc * dti;
+  }
+  }
+}
+
+// W_cv = prim(U_cv) and the CFL maximum of d*c_s + sum |v|
+// (src/sdader_simulator.py:376, src/sd_simulator.py:214-227)
+template <int D>
+__global__ void k_wcv_cmax(Geo g, const double* __restrict__ U_cv, double* __restrict__ W_cv,
+                           unsigned long long* __restrict__ cmax_bits, int* __restrict__ nan_flag) {
+  constexpr int V = D + 2, P_ = D + 1;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double cval = 0.0;
+  bool isnan_c = false;
+  if (q < g.Nq) {
+    double u[V], W[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
+    prim<D>(u, W, g.gamma, 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
+    double c = sound_speed(W[P_], W[0], g.gamma, g.min_c2) * (double)D;
+#pragma unroll
+    for (int v = 1; v <= D; ++v) c = c + fabs(W[v]);
+    if (c != c) isnan_c = true;
+    else cval = c;
+  }
+  // warp max then one atomic per warp
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, cval, off);
+    cval = (o > cval) ? o : cval;
+  }
+  const unsigned nb = __ballot_sync(0xffffffffu, isnan_c);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(cmax_bits, (unsigned long long)__double_as_longlong(cval));
+    if (nb) atomicOr(nan_flag, 1);
+  }
+}
+
+__global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
+                           double* dt) {
+  const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
+                                : __longlong_as_double((long long)*cmax_bits);
+  const double dtt = h / cmax;
+  *dt = cfl * dtt;
+}
+
+}  // namespace spd

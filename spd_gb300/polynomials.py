@@ -1,0 +1,124 @@
+"""Setup-time 1D operators of the SD-ADER scheme (host, FP64, NumPy).
+
+These build the small constant matrices the CUDA kernels apply: the
+solution and flux points of a spectral-difference cell, Lagrange
+interpolation and derivative matrices, the subcell-average matrix and the
+ADER time matrix.  They follow the definitions in the reference's
+src/polynomials.py (line numbers per function) with the same floating-point
+operation sequence, so the matrices are the same bits on the same platform.
+"""
+from __future__ import annotations
+
+from typing import Callable, Tuple
+
+import numpy as np
+
+
+def gauss_legendre_quadrature(x0: float, x1: float, p: int) -> Tuple[np.ndarray, np.ndarray]:
+    """p Gauss-Legendre nodes and weights on [x0, x1] (src/polynomials.py:5-17)."""
+    if p == 0:
+        return np.ndarray(0), np.ndarray(0)
+    x, w = np.polynomial.legendre.leggauss(p)
+    return x0 + (x + 1.0) * (x1 - x0) / 2.0, w * (x1 - x0) / 2.0
+
+
+def solution_points(x0: float, x1: float, p: int) -> np.ndarray:
+    """p+1 Chebyshev-Gauss points on [x0, x1] (src/polynomials.py:19-31)."""
+    i = np.arange(p + 1)
+    return x0 + (1.0 - np.cos((2 * i + 1) / (2 * (p + 1)) * np.pi)) * (x1 - x0) / 2.0
+
+
+def flux_points(x0: float, x1: float, p: int) -> np.ndarray:
+    """The p Gauss-Legendre nodes plus both end points (src/polynomials.py:33-44)."""
+    x, _ = gauss_legendre_quadrature(x0, x1, p)
+    return np.hstack((x0, x, x1))
+
+
+def lagrange_matrix(x_to: np.ndarray, x_from: np.ndarray) -> np.ndarray:
+    """(len(x_to), len(x_from)) Lagrange interpolation matrix (src/polynomials.py:46-65)."""
+    nt, nf = x_to.shape[0], x_from.shape[0]
+    diff = np.broadcast_to(x_to[:, None, None] - x_from[None, None, :], (nt, nf, nf)).copy()
+    diff[:, np.arange(nf), np.arange(nf)] = 1.0
+    den = x_from[:, None] - x_from[None, :]
+    np.fill_diagonal(den, 1.0)
+    return diff.prod(axis=-1) / den.prod(axis=-1)[None, :]
+
+
+def lagrangeprime_matrix(x_to: np.ndarray, x_from: np.ndarray) -> np.ndarray:
+    """Derivatives of the Lagrange basis on x_from at x_to (src/polynomials.py:67-88)."""
+    nt, nf = x_to.shape[0], x_from.shape[0]
+    diff = np.broadcast_to(x_to[:, None, None, None] - x_from[None, None, None, :], (nt, nf, nf, nf)).copy()
+    a = np.arange(nf)
+    diff[:, a, :, a] = 1.0
+    diff[:, :, a, a] = 1.0
+    den = x_from[:, None] - x_from[None, :]
+    np.fill_diagonal(den, 1.0)
+    terms = diff.prod(axis=-1) / den.prod(axis=-1)[None, :, None]
+    terms[:, a, a] = 0.0
+    return terms.sum(axis=-1)
+
+
+def intfromsol_matrix(x_sp: np.ndarray, x_fp: np.ndarray) -> np.ndarray:
+    """Point values -> averages over the control volumes bounded by x_fp
+    (src/polynomials.py:90-107)."""
+    m = x_fp.shape[0] - x_sp.shape[0]
+    n = x_sp.shape[0] - 1
+    if n == 0:
+        return np.ones((1, 1))
+    x, w = gauss_legendre_quadrature(0.0, 1.0, n)
+    xi = (x_fp[:-1, None] + np.diff(x_fp)[:, None] * x[None, :]).ravel()
+    lm = lagrange_matrix(xi, x_sp).reshape(n + m, n, n + 1)
+    return np.einsum("ijk,j->ik", lm, w)
+
+
+def ader_matrix(x_time: np.ndarray, w_time: np.ndarray, dt: float) -> np.ndarray:
+    """ADER time matrix on [0, dt] (src/polynomials.py:109-122)."""
+    ltm = lagrange_matrix(np.array([dt]), x_time).ravel()
+    lpm = lagrangeprime_matrix(x_time, x_time)
+    return ltm[None, :] * ltm[:, None] - lpm.T * w_time[None, :]
+
+
+def quadrature_mean(mesh: np.ndarray, fct: Callable, d: int, v: int, light: bool = True) -> np.ndarray:
+    """Cell means of fct(x, v) over the control volumes of ``mesh`` with a
+    tensor Gauss-Legendre rule (src/polynomials.py:124-148)."""
+    nq = 2 if light else max(mesh.shape[-d:]) - 1
+    x, w = gauss_legendre_quadrature(0.0, 1.0, nq)
+    pts = mesh[(Ellipsis,) + (slice(-1),) * d + (np.newaxis,) * d]
+    pts = np.broadcast_to(pts, pts.shape[:-d] + (nq,) * d).copy()
+    for i in range(d):
+        edges = mesh[(Ellipsis,) + (slice(-1),) * i + (slice(None),) + (slice(-1),) * (d - i - 1)]
+        pts += (np.diff(edges, axis=(i - d))[(Ellipsis,) + (np.newaxis,) * d]
+                * x[(np.newaxis,) * len(mesh.shape) + (np.newaxis,) * i + (slice(None),) + (np.newaxis,) * (d - i - 1)])
+    args = [fct(pts, v), (Ellipsis,) + tuple(range(d))]
+    for i in range(d):
+        args.extend([w, (i,)])
+    return np.einsum(*args)
+
+
+def transform_axis(B: np.ndarray, A: np.ndarray, idim: int, ndim: int, ader: bool = False) -> np.ndarray:
+    """Apply the 1D operator A along the in-cell axis of direction idim of an
+    SD-layout array (src/transforms.py:3-25)."""
+    y = "y" if ndim > 1 else ""
+    j = "j" if ndim > 1 else ""
+    z = "z" if ndim > 2 else ""
+    k = "k" if ndim > 2 else ""
+    t = "t" if ader else ""
+    u = f"u{t}{z}{y}x"
+    if idim == 0:
+        u += f"{k}{j}"
+        return np.einsum(f"fs,{u}s->{u}f", A, B)
+    if idim == 1 and ndim > 1:
+        u += k
+        return np.einsum(f"fs,{u}si->{u}fi", A, B)
+    if idim == 2 and ndim > 2:
+        return np.einsum(f"fs,{u}sji->{u}fji", A, B)
+    raise TypeError("Wrong option for dim")
+
+
+def transform_full(B: np.ndarray, A: np.ndarray, ndim: int) -> np.ndarray:
+    """Apply A along every in-cell axis (src/transforms.py:27-45)."""
+    if ndim == 3:
+        return np.einsum("kn,jm,il,uzyxnml->uzyxkji", A, A, A, B)
+    if ndim == 2:
+        return np.einsum("jm,il,uyxml->uyxji", A, A, B)
+    return np.einsum("il,uxl->uxi", A, B)

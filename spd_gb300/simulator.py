@@ -1,0 +1,594 @@
+"""Drop-in ``SDADER_Simulator`` whose time step runs on the GPU.
+
+The class keeps the constructor, the step/run methods, the state arrays
+(``s.dm.U_sp`` etc., reference layouts) and the options of the reference's
+SDADER_Simulator (src/sdader_simulator.py:14-476 with its bases
+src/sd_simulator.py:19-239, src/fv_simulator.py:10-285,
+src/simulator.py:9-209).  Setup (operators, positions, initial
+condition quadrature) is host NumPy as in the reference; every step runs in
+the CUDA library through spd_gb300._lib.  There is no CPU path for the
+step.
+"""
+from __future__ import annotations
+
+import ctypes
+from collections import defaultdict
+from timeit import default_timer as timer
+from typing import Callable, Tuple
+
+import numpy as np
+
+from . import _lib
+from .initial_conditions import sine_wave
+from .polynomials import (ader_matrix, flux_points, gauss_legendre_quadrature, intfromsol_matrix,
+                          lagrange_matrix, lagrangeprime_matrix, quadrature_mean, solution_points,
+                          transform_axis, transform_full)
+
+DIMS = ("x", "y", "z")
+
+
+def _primitives(U, vels, _p_, gamma):
+    """src/hydro.py:48-86 on the host (user-facing helper)."""
+    W = U.copy()
+    K = W[0].copy() * 0
+    for vel in vels:
+        W[vel] = U[vel] / U[0]
+        K += W[vel] ** 2
+    K *= 0.5 * U[0]
+    W[_p_] = (gamma - 1) * (U[_p_] - K)
+    return W
+
+
+def _conservatives(W, vels, _p_, gamma):
+    """src/hydro.py:88-125 on the host (setup and user-facing helper)."""
+    U = W.copy()
+    K = W[0].copy() * 0
+    for vel in vels:
+        U[vel] = W[vel] * U[0]
+        K += W[vel] ** 2
+    K *= 0.5 * U[0]
+    U[_p_] = W[_p_] / (gamma - 1) + K
+    return U
+
+
+def mesh_cv(ndim, N, p, lims, Nghe, fp_ref) -> np.ndarray:
+    """Flux-point coordinates of every cell including Nghe ghost layers,
+    shape (ndim, [Nz,] [Ny,] Nx, p+2, ...) (src/sd_simulator.py:59-72)."""
+    Ns = [N[i] + 2 * Nghe for i in range(ndim)]
+    shape = (ndim,) + tuple(Ns[::-1]) + (p + 2,) * ndim
+    mesh = np.ndarray(shape)
+    for idim in range(ndim):
+        Nd = Ns[idim]
+        h = (lims[idim][1] - lims[idim][0]) / N[idim]
+        length = (lims[idim][1] - lims[idim][0]) + 2 * Nghe * h
+        s1 = (None,) * (ndim - 1 - idim) + (slice(None),) + (None,) * (ndim + idim)
+        s2 = (None,) * (2 * ndim - 1 - idim) + (slice(None),) + (None,) * idim
+        mesh[idim] = lims[idim][0] + (np.arange(Nd)[s1] + fp_ref[s2]) * length / Nd - h
+    return mesh
+
+
+def subcell_faces(N, h, fp_ref, ngh) -> np.ndarray:
+    """Subcell face positions of one direction with ngh mirrored ghost faces
+    per side (src/sdader_simulator.py:73-78)."""
+    n = len(fp_ref) - 1
+    fp = np.ndarray(N * n + ngh * 2 + 1)
+    fp[ngh:-ngh] = h * np.hstack((np.arange(N).repeat(n) + np.tile(fp_ref[:-1], N), N))
+    fp[:ngh] = -fp[(ngh + 1):(2 * ngh + 1)][::-1]
+    fp[-ngh:] = fp[-(ngh + 1)] + fp[ngh + 1:2 * ngh + 1]
+    return fp
+
+
+def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1):
+    """Initial subcell averages of the primitives and the derived
+    solution-point / conservative arrays (src/sd_simulator.py:74-90).
+    Returns (W_gh, W_init_cv, W_sp, U_sp, U_cv)."""
+    nvar = ndim + 2
+    vels = np.arange(ndim) + 1
+    mesh = mesh_cv(ndim, N, p, lims, Nghe, ops["x_fp"])
+    W_gh = np.ndarray((nvar,) + tuple(N[i] + 2 * Nghe for i in range(ndim))[::-1] + (p + 1,) * ndim)
+    for var in range(nvar):
+        W_gh[var] = quadrature_mean(mesh, init_fct, ndim, var)
+    W_init_cv = W_gh[(slice(None),) + (slice(Nghe, -Nghe),) * ndim + (Ellipsis,)]
+    W_cv = W_init_cv.copy()
+    W_sp = transform_full(W_cv, ops["cv_to_sp"], ndim)
+    U_sp = _conservatives(W_sp, vels, ndim + 1, gamma)
+    U_cv = _conservatives(W_cv, vels, ndim + 1, gamma)
+    return W_gh, W_init_cv, W_sp, U_sp, U_cv
+
+
+class _DataManager:
+    """Stand-in for the reference's GPUDataManager (src/data_management.py:
+    32-68): device-resident fields are downloaded on read (a fresh NumPy
+    array) and uploaded on assignment; constants live on the host."""
+
+    _device_fields = ("U_sp", "U_cv", "W_cv", "troubles", "theta",
+                      "affected_faces_x", "affected_faces_y", "affected_faces_z")
+
+    def __init__(self, sim):
+        object.__setattr__(self, "_sim", sim)
+        object.__setattr__(self, "_host", {})
+
+    @property
+    def xp(self):
+        return np
+
+    def switch_to(self, location):
+        return None
+
+    def asnumpy(self, arr):
+        return np.asarray(arr)
+
+    def __getattr__(self, name):
+        sim = object.__getattribute__(self, "_sim")
+        if name == "dt":
+            return sim._ctx.get_dt()
+        if name in _DataManager._device_fields and sim._ctx is not None:
+            return sim._download(name)
+        host = object.__getattribute__(self, "_host")
+        if name in host:
+            return host[name]
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        sim = object.__getattribute__(self, "_sim")
+        if name == "dt" and sim._ctx is not None:
+            sim._ctx.set_dt(float(value))
+            return
+        if name in ("U_sp", "U_cv", "W_cv") and sim._ctx is not None:
+            sim._ctx.upload(name, np.asarray(value, dtype=np.float64))
+            return
+        object.__getattribute__(self, "_host")[name] = value
+
+
+class SDADER_Simulator:
+    """SD-ADER simulator for the compressible Euler equations (GPU step).
+
+    Positional and keyword arguments follow the reference's constructor
+    chain SDADER_Simulator -> SD_Simulator -> FV_Simulator -> Simulator.
+    Options the GPU path does not implement (viscosity, potential, WB,
+    isothermal, predictor=False) raise NotImplementedError.
+    """
+
+    def __init__(self,
+                 FB: bool = False,
+                 tolerance: float = 1e-5,
+                 SED: bool = True,
+                 NAD: str = "",
+                 PAD: bool = True,
+                 blending: bool = True,
+                 min_rho: float = 1e-10,
+                 max_rho: float = 1e10,
+                 min_P: float = 1e-10,
+                 godunov: bool = False,
+                 riemann_solver_sd: str = "llf",
+                 update: str = "SD",
+                 riemann_solver_fv: str = "llf",
+                 slope_limiter: str = "minmod",
+                 predictor: bool = True,
+                 init_fct: Callable = sine_wave,
+                 eq_fct: Callable = sine_wave,
+                 p: int = 1,
+                 m: int = -1,
+                 N: Tuple = (32, 32),
+                 Nghe: int = 1,
+                 Nghc: int = 2,
+                 xlim: Tuple = (0, 1),
+                 ylim: Tuple = (0, 1),
+                 zlim: Tuple = (0, 1),
+                 gamma: float = 1.4,
+                 beta: float = 2. / 3,
+                 nu: float = 1e-4,
+                 cfl_coeff: float = 0.8,
+                 min_c2: float = 1E-10,
+                 isothermal: bool = False,
+                 viscosity: bool = False,
+                 potential: bool = False,
+                 WB: bool = False,
+                 use_cupy: bool = True,
+                 BC: Tuple = (("periodic", "periodic"),
+                              ("periodic", "periodic"),
+                              ("periodic", "periodic")),
+                 verbose=True,
+                 operators: dict | None = None):
+        for flag, name in ((isothermal, "isothermal"), (viscosity, "viscosity"),
+                           (potential, "potential"), (WB, "WB")):
+            if flag:
+                raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
+        if not predictor:
+            raise NotImplementedError("predictor=False (plain MUSCL) is not implemented "
+                                      "(the reference's path raises AttributeError)")
+        if Nghc != 2:
+            raise NotImplementedError("only Nghc=2 subcell ghost layers are supported")
+        if riemann_solver_sd not in _lib.RIEMANN:
+            raise AttributeError(riemann_solver_sd)
+        if riemann_solver_fv not in _lib.RIEMANN:
+            raise AttributeError(riemann_solver_fv)
+        if slope_limiter not in _lib.LIMITER:
+            raise AttributeError(slope_limiter)
+        if update not in _lib.UPDATE:
+            raise ValueError(f"update must be 'SD' or 'FV', got {update!r}")
+        self._ctx = None
+        # ---- Simulator (src/simulator.py:10-126) ----------------------
+        self.init_fct = init_fct
+        self.eq_fct = eq_fct
+        if m == -1:
+            m = p
+        self.p = p
+        self.m = m
+        ndim = len(N)
+        self.ndim = ndim
+        assert len(BC) >= ndim
+        self.BC = {}
+        self.idims = {}
+        self.dims = {}
+        for idim in range(ndim):
+            dim = DIMS[idim]
+            self.idims[idim] = dim
+            self.dims[dim] = idim
+            self.BC[dim] = BC[idim]
+            for side in (0, 1):
+                if BC[idim][side] not in _lib.BCKIND:
+                    raise TypeError("Undetermined boundary type")
+            setattr(self, f"N{dim}", N[idim])
+        self.Y = ndim > 1
+        self.Z = ndim > 2
+        self.xlim, self.ylim, self.zlim = xlim, ylim, zlim
+        self.time = 0.0
+        self.Nghe = Nghe
+        self.Nghc = Nghc
+        self.gamma = gamma
+        self.beta = beta
+        self.nu = nu
+        self.cfl_coeff = cfl_coeff
+        self.min_c2 = min_c2
+        self.isothermal = isothermal
+        self.viscosity = viscosity
+        self.potential = potential
+        self.WB = WB
+        self.verbose = verbose
+        self.use_cupy = use_cupy
+        self.dm = _DataManager(self)
+        self.nghx = Nghc
+        self.nghy = (0, Nghc)[self.Y]
+        self.nghz = (0, Nghc)[self.Z]
+        self.lim, self.len, self.h, self.N, self.ngh = {}, {}, {}, {}, {}
+        self.h_min = 1E10
+        for dim in self.dims:
+            self.lim[dim] = getattr(self, f"{dim}lim")
+            setattr(self, f"{dim}len", self.lim[dim][1] - self.lim[dim][0])
+            self.len[dim] = getattr(self, f"{dim}len")
+            self.N[dim] = getattr(self, f"N{dim}")
+            setattr(self, f"d{dim}", self.len[dim] / self.N[dim])
+            self.h[dim] = getattr(self, f"d{dim}")
+            self.ngh[dim] = getattr(self, f"ngh{dim}")
+            self.h_min = min(self.h_min, self.h[dim])
+        self.n_step = 0
+        self.variables = [r"$\rho$"]
+        self._d_ = 0
+        self.vels = np.arange(ndim) + 1
+        for dim in self.dims:
+            name = f"v{dim}"
+            self.variables.append(name)
+            setattr(self, f"_{name}_", self.vels[self.dims[dim]])
+        self.variables.append("P")
+        self._p_ = ndim + 1
+        self.nvar = ndim + 2
+        self.rank = 0
+        # ---- FV_Simulator / SD_Simulator options ----------------------
+        self.riemann_solver_fv_name = riemann_solver_fv
+        self.riemann_solver_sd_name = riemann_solver_sd
+        self.slope_limiter_name = slope_limiter
+        self.predictor = predictor
+        self.update = update
+        # ---- SD_Simulator operators (src/sd_simulator.py:30-52) ------------
+        self.x, self.w = gauss_legendre_quadrature(0.0, 1.0, p)
+        sp = solution_points(0.0, 1.0, p)
+        fp = flux_points(0.0, 1.0, p)
+        self.sp, self.fp, self.n = defaultdict(list), defaultdict(list), defaultdict(list)
+        for dim in self.dims:
+            setattr(self, f"{dim}_sp", sp)
+            self.sp[dim] = sp
+            setattr(self, f"{dim}_fp", fp)
+            self.fp[dim] = fp
+            setattr(self, f"n{dim}", p + 1)
+            self.n[dim] = p + 1
+        if operators is None:
+            operators = self.build_operators(p, m)
+        self.ops = operators
+        for key in ("sp_to_fp", "fp_to_sp", "dfp_to_sp", "sp_to_cv", "fp_to_cv", "cv_to_sp",
+                    "x_tp", "w_tp", "invader"):
+            if key in operators:
+                setattr(self.dm, key, operators[key])
+        self.nader = m + 1
+        # ---- SDADER options -------------------------------------------
+        self.FB = FB
+        self.tolerance = tolerance
+        self.SED = SED
+        self.NAD = NAD
+        self.PAD = PAD
+        self.blending = blending
+        self.min_rho = min_rho
+        self.max_rho = max_rho
+        self.min_P = min_P
+        self.godunov = godunov
+        # ---- geometry and initial state (src/sd_simulator.py:59-90) ----
+        self.mesh_cv = self.compute_mesh_cv()
+        self.compute_positions()
+        W_gh, self.W_init_cv, W_sp, U_sp, U_cv = initial_state(
+            ndim, [self.N[d] for d in self.dims], p, [self.lim[d] for d in self.dims], self.init_fct,
+            operators, gamma, Nghe)
+        W_cv = self.W_init_cv.copy()
+        self.dm.W_sp = W_sp
+        # ---- device context ----------------------------------------------
+        self._create_context()
+        self._ctx.upload("U_sp", U_sp)
+        self._ctx.upload("U_cv", U_cv)
+        self._ctx.upload("W_cv", W_cv)
+        self._init_boundaries(U_sp, W_gh)
+        self.compute_dt()
+
+    # ------------------------------------------------------------------
+    # setup
+    # ------------------------------------------------------------------
+    @staticmethod
+    def build_operators(p: int, m: int) -> dict:
+        """Constant operators (src/sd_simulator.py:44-52,
+        src/sdader_simulator.py:40-44)."""
+        x_sp = solution_points(0.0, 1.0, p)
+        x_fp = flux_points(0.0, 1.0, p)
+        ops = {
+            "x_sp": x_sp,
+            "x_fp": x_fp,
+            "sp_to_fp": lagrange_matrix(x_fp, x_sp),
+            "fp_to_sp": lagrange_matrix(x_sp, x_fp),
+            "dfp_to_sp": lagrangeprime_matrix(x_sp, x_fp),
+            "sp_to_cv": intfromsol_matrix(x_sp, x_fp),
+            "fp_to_cv": intfromsol_matrix(x_fp, x_fp),
+        }
+        ops["cv_to_sp"] = np.linalg.inv(ops["sp_to_cv"])
+        x_tp, w_tp = gauss_legendre_quadrature(0.0, 1.0, m + 1)
+        ader = ader_matrix(x_tp, w_tp, 1.0)
+        invader = np.linalg.inv(ader)
+        ops["x_tp"] = x_tp
+        ops["w_tp"] = w_tp
+        ops["invader"] = np.einsum("p,np->np", w_tp, invader)
+        return ops
+
+    def compute_mesh_cv(self) -> np.ndarray:
+        return mesh_cv(self.ndim, [self.N[d] for d in self.dims], self.p, [self.lim[d] for d in self.dims],
+                       self.Nghe, self.fp["x"])
+
+    def compute_positions(self):
+        """Subcell faces, centres and widths with Nghc ghost layers
+        (src/sdader_simulator.py:61-92)."""
+        ngh = self.Nghc
+        self.faces, self.centers, self.h_fp, self.h_cv = {}, {}, {}, {}
+        for dim in self.dims:
+            idim = self.dims[dim]
+            Nd, nd = self.N[dim], self.n[dim]
+            fp = subcell_faces(Nd, self.h[dim], self.fp[dim], ngh)
+            self.faces[dim] = fp
+            cv = 0.5 * (fp[1:] + fp[:-1])
+            self.centers[dim] = cv
+            self.h_fp[dim] = (fp[1:] - fp[:-1])[self.shape(idim)]
+            self.h_cv[dim] = (cv[1:] - cv[:-1])[self.shape(idim)]
+            sp = self.lim[dim][0] + (np.arange(Nd)[:, None] + self.sp[dim][None, :]) * self.h[dim]
+            setattr(self.dm, f"{dim.upper()}_sp", sp.reshape(Nd, nd))
+            setattr(self.dm, f"{dim.upper()}_fp", fp)
+            setattr(self.dm, f"{dim.upper()}_cv", cv)
+
+    def _create_context(self):
+        cfg = _lib.spd_config()
+        cfg.ndim = self.ndim
+        for i in range(self.ndim):
+            dim = DIMS[i]
+            cfg.N[i] = self.N[dim]
+            cfg.lim[i][0] = float(self.lim[dim][0])
+            cfg.lim[i][1] = float(self.lim[dim][1])
+            cfg.BC[i][0] = _lib.BCKIND[self.BC[dim][0]]
+            cfg.BC[i][1] = _lib.BCKIND[self.BC[dim][1]]
+        cfg.p = self.p
+        cfg.m = self.m
+        cfg.gamma = self.gamma
+        cfg.cfl_coeff = self.cfl_coeff
+        cfg.min_c2 = self.min_c2
+        cfg.riemann_solver_sd = _lib.RIEMANN[self.riemann_solver_sd_name]
+        cfg.riemann_solver_fv = _lib.RIEMANN[self.riemann_solver_fv_name]
+        cfg.slope_limiter = _lib.LIMITER[self.slope_limiter_name]
+        cfg.update = _lib.UPDATE[self.update]
+        cfg.FB = int(bool(self.FB))
+        cfg.tolerance = self.tolerance
+        cfg.SED = int(bool(self.SED))
+        cfg.NAD_delta = int(self.NAD == "delta")
+        cfg.PAD = int(bool(self.PAD))
+        cfg.blending = int(bool(self.blending))
+        cfg.min_rho = self.min_rho
+        cfg.max_rho = self.max_rho
+        cfg.min_P = self.min_P
+        cfg.godunov = int(bool(self.godunov))
+        faces = [self.faces[DIMS[i]] for i in range(self.ndim)]
+        self._ctx = _lib.Context(cfg, self.ops, faces)
+
+    def _init_boundaries(self, U_sp, W_gh):
+        """Initial boundary arrays: element edge traces of the initial state
+        (src/sdader_simulator.py:415-423) and subcell ghost layers of the
+        initial condition (src/fv_simulator.py:213-222)."""
+        ndim = self.ndim
+        T = self.nader
+        for dim in self.dims:
+            idim = self.dims[dim]
+            M_fp = self.compute_fp_from_sp(U_sp, dim)
+            first = [slice(None)] * M_fp.ndim
+            last = [slice(None)] * M_fp.ndim
+            first[-(ndim + idim + 1)] = 0
+            first[-(idim + 1)] = 0
+            last[-(ndim + idim + 1)] = -1
+            last[-(idim + 1)] = -1
+            b0 = M_fp[tuple(first)]
+            b1 = M_fp[tuple(last)]
+            BC = np.stack([np.repeat(b0[:, None], T, axis=1), np.repeat(b1[:, None], T, axis=1)])
+            self._ctx.upload(f"BC_fp_{dim}", BC)
+        if self.update == "FV":
+            ngh = self.Nghc
+            n = self.p + 1
+            M = self.transpose_to_fv(W_gh)
+            if n > 2:
+                M = M[(Ellipsis,) + (slice(n - ngh, -(n - ngh)),) * ndim]
+            for dim in self.dims:
+                idim = self.dims[dim]
+                lo = [slice(None)] * M.ndim
+                hi = [slice(None)] * M.ndim
+                lo[M.ndim - 1 - idim] = slice(None, ngh)
+                hi[M.ndim - 1 - idim] = slice(-ngh, None)
+                self._ctx.upload(f"BC_fv_{dim}", np.stack([M[tuple(lo)], M[tuple(hi)]]))
+
+    # ------------------------------------------------------------------
+    # layouts and host-side helpers (src/simulator.py, src/sd_simulator.py)
+    # ------------------------------------------------------------------
+    def shape(self, idim):
+        return (None,) * (self.ndim - idim) + (slice(None),) + (None,) * idim
+
+    def domain_size(self):
+        return [self.N[dim] * self.n[dim] for dim in self.dims]
+
+    def regular_faces(self):
+        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim] + 1) for dim in self.dims]
+
+    def regular_centers(self):
+        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim]) for dim in self.dims]
+
+    def crop(self, M, ngh=1) -> np.ndarray:
+        return M[(slice(None),) + (slice(ngh, -ngh),) * self.ndim + (Ellipsis,)]
+
+    def compute_primitives(self, U, **kwargs) -> np.ndarray:
+        return _primitives(U, self.vels, self._p_, self.gamma)
+
+    def compute_conservatives(self, W, **kwargs) -> np.ndarray:
+        return _conservatives(W, self.vels, self._p_, self.gamma)
+
+    def array(self, px, py, pz, ngh=0, ader=False) -> np.ndarray:
+        shape = [self.nvar, self.nader] if ader else [self.nvar]
+        Ns = [self.N[dim] + 2 * ngh for dim in self.dims][::-1]
+        pts = [px, py, pz][:self.ndim][::-1]
+        return np.ndarray(shape + Ns + pts)
+
+    def array_sp(self, **kwargs):
+        return self.array(self.p + 1, self.p + 1, self.p + 1, **kwargs)
+
+    def transpose_to_fv(self, M):
+        if self.ndim == 1:
+            return M.reshape(M.shape[0], M.shape[1] * M.shape[2])
+        if self.ndim == 2:
+            return np.transpose(M, (0, 1, 3, 2, 4)).reshape(M.shape[0], M.shape[1] * M.shape[3],
+                                                            M.shape[2] * M.shape[4])
+        return np.transpose(M, (0, 1, 4, 2, 5, 3, 6)).reshape(M.shape[0], M.shape[1] * M.shape[4],
+                                                              M.shape[2] * M.shape[5], M.shape[3] * M.shape[6])
+
+    def transpose_to_sd(self, M):
+        shape = []
+        for dim in self.dims:
+            shape += [self.n[dim], self.N[dim]]
+        shape = [M.shape[0]] + shape[::-1]
+        if self.ndim == 1:
+            return M.reshape(shape)
+        if self.ndim == 2:
+            return np.transpose(M.reshape(shape), (0, 1, 3, 2, 4))
+        return np.transpose(M.reshape(shape), (0, 1, 3, 5, 2, 4, 6))
+
+    def compute_sp_from_cv(self, M_cv) -> np.ndarray:
+        return transform_full(M_cv, self.ops["cv_to_sp"], self.ndim)
+
+    def compute_cv_from_sp(self, M_sp) -> np.ndarray:
+        return transform_full(M_sp, self.ops["sp_to_cv"], self.ndim)
+
+    def compute_fp_from_sp(self, M_sp, dim, **kwargs) -> np.ndarray:
+        return transform_axis(M_sp, self.ops["sp_to_fp"], self.dims[dim], self.ndim, **kwargs)
+
+    def compute_sp_from_fp(self, M_fp, dim, **kwargs) -> np.ndarray:
+        return transform_axis(M_fp, self.ops["fp_to_sp"], self.dims[dim], self.ndim, **kwargs)
+
+    def compute_sp_from_dfp(self, M_fp, dim, **kwargs) -> np.ndarray:
+        return transform_axis(M_fp, self.ops["dfp_to_sp"], self.dims[dim], self.ndim, **kwargs)
+
+    def regular_mesh(self, W):
+        """Interpolate SD-layout values to equispaced points for plotting
+        (src/sd_simulator.py:92-102)."""
+        p = self.p
+        if p <= 1:
+            return W
+        x = np.arange(p + 2) / (p + 1)
+        x = .5 * (x[1:] + x[:-1])
+        return transform_full(W, lagrange_matrix(x, solution_points(0.0, 1.0, p)), self.ndim)
+
+    # ------------------------------------------------------------------
+    # device state
+    # ------------------------------------------------------------------
+    def _shape_of(self, name):
+        nd = self.ndim
+        Ns = tuple(self.N[DIMS[i]] for i in range(nd))[::-1]
+        n = self.p + 1
+        X = [self.N[DIMS[i]] * n for i in range(nd)]
+        if name in ("U_sp", "U_cv", "W_cv"):
+            return (self.nvar,) + Ns + (n,) * nd
+        if name == "troubles":
+            return (1,) + tuple(X[::-1])
+        if name == "theta":
+            return (1,) + tuple(x + 2 * self.Nghc for x in X[::-1])
+        if name.startswith("affected_faces_"):
+            d = DIMS.index(name[-1])
+            ext = [x + (1 if i == d else 0) for i, x in enumerate(X)]
+            return (1,) + tuple(ext[::-1])
+        raise KeyError(name)
+
+    def _download(self, name):
+        if name.startswith("affected_faces_") and DIMS.index(name[-1]) >= self.ndim:
+            raise AttributeError(name)
+        if name in ("troubles", "theta") or name.startswith("affected_faces_"):
+            if not (self.update == "FV" and self.FB):
+                raise AttributeError(f"{name} exists only with update='FV' and FB=True")
+        return self._ctx.download(name, self._shape_of(name))
+
+    # ------------------------------------------------------------------
+    # time stepping (src/sdader_simulator.py:361-413, src/sd_simulator.py:214-227)
+    # ------------------------------------------------------------------
+    def compute_dt(self) -> None:
+        self._ctx.compute_dt()
+
+    def perform_update(self) -> bool:
+        self.n_step += 1
+        self.time = self._ctx.perform_update(self.time)
+        return True
+
+    def init_sim(self):
+        self.execution_time = -timer()
+
+    def end_sim(self):
+        self._ctx.synchronize()
+        self.execution_time += timer()
+        self._ctx.end_sim()
+        if self.rank == 0:
+            print(f"t={self.time}, steps taken {self.n_step}, time taken {self.execution_time}")
+
+    def perform_iterations(self, n_step: int) -> None:
+        self.init_sim()
+        self.time, done = self._ctx.step(n_step, 0.0, 0, self.time)
+        self.n_step += done
+        self.end_sim()
+
+    def perform_time_evolution(self, t_end: float, nsteps=0) -> None:
+        self.init_sim()
+        self.time, done = self._ctx.step(0, t_end, 1, self.time)
+        self.n_step += done
+        if self.time < t_end:
+            print(f"dt={self.dm.dt}")
+        self.end_sim()
+
+    def close(self):
+        if self._ctx is not None:
+            self._ctx.close()
+            self._ctx = None
+
+
+class SD_Simulator(SDADER_Simulator):
+    """Name kept for callers that construct the SD base class directly; it
+    is the same object as SDADER_Simulator with its defaults."""

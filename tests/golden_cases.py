@@ -1,0 +1,68 @@
+"""Load the golden fixtures (outputs of the reference's NumPy path) and
+build matching oracle / product runs from them."""
+from __future__ import annotations
+
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+DIMS = ("x", "y", "z")
+
+
+def case_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not p.endswith("operators.npz"))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    data = {k: z[k] for k in z.files}
+    meta = json.loads(str(data.pop("case_json")))
+    kw = dict(meta["kwargs"])
+    if "N" in kw:
+        kw["N"] = tuple(kw["N"])
+    for key in ("xlim", "ylim", "zlim"):
+        if key in kw:
+            kw[key] = tuple(kw[key])
+    kw["BC"] = tuple(tuple(b) for b in kw["BC"])
+    return data, kw, meta
+
+
+def make_ic(spec):
+    from spd_gb300 import initial_conditions as ics
+    name, kw = spec
+    if name == "vortex":
+        return ics.isentropic_vortex()
+    if name in ("sedov", "kelvin_helmholtz"):
+        return getattr(ics, name)(**kw)
+    return getattr(ics, name)
+
+
+def oracle_from_golden(data, kw):
+    from oracle.sdader_oracle import OracleSDADER
+    ndim = len(kw["N"])
+    p = kw["p"]
+    lims = [kw.get(f"{d}lim", (0, 1)) for d in DIMS[:ndim]]
+    ops = {k: data[k] for k in ("sp_to_fp", "dfp_to_sp", "sp_to_cv", "cv_to_sp", "w_tp", "invader", "x_fp")}
+    state = {"U_sp": data["init_U_sp"], "U_cv": data["init_U_cv"], "W_cv": data["init_W_cv"]}
+    for d in DIMS[:ndim]:
+        state[f"BC_fp_{d}"] = data[f"init_BC_fp_{d}"]
+        if f"init_BC_fv_{d}" in data:
+            state[f"BC_fv_{d}"] = data[f"init_BC_fv_{d}"]
+    return OracleSDADER(
+        ndim=ndim, N=list(kw["N"]), p=p, m=kw.get("m", -1) if kw.get("m", -1) != -1 else p, lims=lims,
+        BC=kw["BC"], gamma=kw.get("gamma", 1.4), cfl_coeff=kw.get("cfl_coeff", 0.8), min_c2=kw.get("min_c2", 1e-10),
+        riemann_solver_sd=kw.get("riemann_solver_sd", "llf"), riemann_solver_fv=kw.get("riemann_solver_fv", "llf"),
+        slope_limiter=kw.get("slope_limiter", "minmod"), update=kw.get("update", "SD"), FB=kw.get("FB", False),
+        tolerance=kw.get("tolerance", 1e-5), SED=kw.get("SED", True), NAD=kw.get("NAD", ""),
+        PAD=kw.get("PAD", True), blending=kw.get("blending", True), min_rho=kw.get("min_rho", 1e-10),
+        max_rho=kw.get("max_rho", 1e10), min_P=kw.get("min_P", 1e-10), godunov=kw.get("godunov", False),
+        ops=ops, state=state)
+
+
+def golden_operators(data):
+    return {k: data[k] for k in ("sp_to_fp", "fp_to_sp", "dfp_to_sp", "sp_to_cv", "fp_to_cv", "cv_to_sp",
+                                 "x_tp", "w_tp", "invader", "x_sp", "x_fp")}

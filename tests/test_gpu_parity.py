@@ -1,0 +1,170 @@
+"""Parity of the CUDA step with the reference (golden fixtures) and with
+the oracle restatement (same inputs, run here).  Floating-point tolerance:
+the kernels reproduce the reference's operation order, so every comparison
+is bitwise (np.array_equal); the 1e-12 / 1e-10 relative bounds of the
+specification are implied."""
+import numpy as np
+import pytest
+
+from golden_cases import DIMS, case_names, golden_operators, load, make_ic
+from gpu_helpers import compare, oracle_like, step_both
+
+pytestmark = pytest.mark.gpu
+
+
+def product_from_golden(data, kw, meta):
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(init_fct=make_ic(meta["ic"]), operators=golden_operators(data), verbose=False, **kw)
+    s.dm.U_sp = data["init_U_sp"]
+    s.dm.U_cv = data["init_U_cv"]
+    s.dm.W_cv = data["init_W_cv"]
+    return s
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_gpu_matches_reference_golden(name):
+    data, kw, meta = load(name)
+    s = product_from_golden(data, kw, meta)
+    dts = []
+    for _ in range(meta["steps"]):
+        s.compute_dt()
+        dts.append(s.dm.dt)
+        s.perform_update()
+    assert np.array_equal(np.array(dts), data["dts"]), (dts, data["dts"])
+    assert s.time == float(data["time"])
+    for key in ("U_sp", "U_cv", "W_cv"):
+        got = getattr(s.dm, key)
+        assert np.array_equal(got, data[key], equal_nan=True), (key, np.nanmax(np.abs(got - data[key])))
+    if "troubles" in data:
+        assert np.array_equal(s.dm.troubles, data["troubles"])
+        assert np.array_equal(s.dm.theta, data["theta"])
+        for d in s.dims:
+            assert np.array_equal(getattr(s.dm, f"affected_faces_{d}"), data[f"affected_faces_{d}"])
+    s.close()
+
+
+def _run_vs_oracle(nsteps, **kw):
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(verbose=False, **kw)
+    o = oracle_like(s)
+    dts = step_both(s, o, nsteps)
+    assert all(a == b for a, b in dts), dts[:3]
+    bad = compare(s, o)
+    troubles = float(s.dm.troubles.sum()) if (s.update == "FV" and s.FB) else 0.0
+    s.close()
+    return bad, troubles
+
+
+def test_vortex_32_p3_100_steps_bitwise():
+    """Isentropic vortex, 32x32 cells, p=3, FV update with limiting, LLF,
+    100 steps (the parity case of the vortex benchmark)."""
+    from spd_gb300.initial_conditions import isentropic_vortex
+    bad, _ = _run_vs_oracle(100, p=3, N=(32, 32), xlim=(0, 10), ylim=(0, 10), init_fct=isentropic_vortex(),
+                            update="FV", FB=True, riemann_solver_sd="llf", riemann_solver_fv="llf",
+                            BC=(("periodic", "periodic"),) * 2)
+    assert not bad, bad
+
+
+def test_quadrant_64_p3_20_steps_bitwise():
+    """Four-quadrant Riemann problem at 64x64 cells (the 512x512 benchmark
+    reduced), transmissive boundaries, HLLC, limiting, 20 steps."""
+    from spd_gb300.initial_conditions import four_quadrant
+    bad, troubles = _run_vs_oracle(20, p=3, N=(64, 64), init_fct=four_quadrant, update="FV", FB=True,
+                                   riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                   BC=(("gradfree", "gradfree"),) * 2)
+    assert troubles > 0
+    assert not bad, bad
+
+
+def test_sedov_16_p2_10_steps_bitwise():
+    """3D Sedov blast at 16^3 cells (the 128^3 benchmark reduced), p=2,
+    reflective walls, HLLC, limiting, 10 steps."""
+    from spd_gb300.initial_conditions import sedov
+    bad, troubles = _run_vs_oracle(10, p=2, N=(16, 16, 16), init_fct=sedov(16), update="FV", FB=True,
+                                   riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                   BC=(("reflective", "reflective"),) * 3)
+    assert troubles > 0
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("p", [1, 3])
+@pytest.mark.parametrize("N", [(6,), (6, 6), (6, 6, 6)])
+@pytest.mark.parametrize("update", ["SD", "FV"])
+@pytest.mark.parametrize("FB", [True, False])
+def test_update_matrix_vs_oracle(p, N, update, FB):
+    """Mirrors the reference's test/test_update.py:10-18 (every dimension,
+    degree, update and limiting flag), with a bitwise check."""
+    bad, _ = _run_vs_oracle(2, p=p, N=N, update=update, FB=FB)
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("p", [1, 3])
+@pytest.mark.parametrize("N", [(6,), (6, 6)])
+@pytest.mark.parametrize("mode", ["SD", "FV", "FB_godunov", "FB"])
+def test_preserve_velocity_and_pressure(p, N, mode):
+    """Mirrors the reference's test/test_preserve.py:10-38: an advected
+    density wave keeps velocity and pressure constant.  The threshold is the
+    reference's 1e-14 (mean absolute); in 2D with p=3 the reference's own
+    NumPy run measures 1.5-1.6e-14 (the same bits as this GPU run), so the
+    test asserts equality with the oracle there and 2e-14."""
+    from spd_gb300 import SDADER_Simulator
+    kw = dict(p=p, N=N, verbose=False)
+    if mode == "FV":
+        kw["update"] = "FV"
+    elif mode == "FB_godunov":
+        kw.update(update="FV", FB=True, godunov=True)
+    elif mode == "FB":
+        kw.update(update="FV", FB=True)
+    s = SDADER_Simulator(**kw)
+    o = oracle_like(s)
+    s.perform_time_evolution(1)
+    o.perform_time_evolution(1)
+    W = s.dm.W_cv
+    assert np.array_equal(W, o.W_cv)
+    assert np.mean(np.abs(W[0] - s.W_init_cv[0])) > 1e-14
+    tol = 2e-14 if (len(N) == 2 and p == 3) else 1e-14
+    assert np.mean(np.abs(W[1:] - s.W_init_cv[1:])) < tol
+    s.close()
+
+
+@pytest.mark.parametrize("p", [1, 3])
+@pytest.mark.parametrize("N", [(6,), (6, 6), (6, 6, 6)])
+def test_create(p, N):
+    """Mirrors the reference's test/test_create.py:12-16."""
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(p=p, N=N, verbose=False)
+    assert s.dm.U_sp.shape == (len(N) + 2,) + N + (p + 1,) * len(N)
+    s.close()
+
+
+def test_vortex_t1_error_against_exact():
+    """Vortex benchmark run to t=1: L1 error of the subcell-averaged density
+    against the exact (translated) solution, and the same bits as the oracle."""
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import isentropic_vortex
+    from spd_gb300.polynomials import quadrature_mean
+    kw = dict(p=3, N=(32, 32), xlim=(0, 10), ylim=(0, 10), update="FV", FB=True, riemann_solver_sd="llf",
+              riemann_solver_fv="llf", BC=(("periodic", "periodic"),) * 2, verbose=False)
+    s = SDADER_Simulator(init_fct=isentropic_vortex(), **kw)
+    o = oracle_like(s)
+    s.perform_time_evolution(1.0)
+    o.perform_time_evolution(1.0)
+    assert s.n_step == 87
+    assert np.array_equal(s.dm.U_sp, o.U_sp)
+    exact = s.crop(quadrature_mean(s.mesh_cv, isentropic_vortex(center=(6.0, 6.0)), 2, 0, light=False)[None])[0]
+    err = float(np.mean(np.abs(s.dm.W_cv[0] - exact)))
+    assert 1.0e-6 < err < 2.0e-6, err  # the reference's NumPy run gives 1.556e-6
+    assert float(s.dm.troubles.sum()) == 0.0
+    s.close()
+
+
+@pytest.mark.slow
+def test_quadrant_512_one_step_full_size_bitwise():
+    """The 512x512 four-quadrant benchmark at full size: one step bitwise
+    against the oracle (the oracle needs ~10 GB and a minute or two)."""
+    from spd_gb300.initial_conditions import four_quadrant
+    bad, troubles = _run_vs_oracle(1, p=3, N=(512, 512), init_fct=four_quadrant, update="FV", FB=True,
+                                   riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                   BC=(("gradfree", "gradfree"),) * 2)
+    assert troubles > 0
+    assert not bad, bad
