@@ -1,0 +1,376 @@
+"""Throughput of the GB300 SD-ADER step: FP64 DOF-updates/s.
+
+Default workload: the four-quadrant 2D Riemann problem on [0,1]^2 with
+transmissive boundaries, 512x512 cells, p=3 (16 solution points per cell),
+HLLC, NAD/SED/PAD trouble detection with MUSCL-Hancock fallback on
+(p+1)^2 subcells.  One step = compute_dt + perform_update (the body of
+SDADER_Simulator.perform_iterations).  DOF = cells * (p+1)^2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference's NumPy path on the host cores (one independent instance per
+core) on a bounded sample of the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 DOF-updates/s on 1 GB300 (p=3)"
+UNIT = "DOF-updates/s"
+
+WORKLOADS = {
+    # name: (description, constructor kwargs factory)
+    "quadrant512": "four-quadrant Riemann problem, 512x512 cells, p=3, FV update with NAD/SED/PAD limiting and "
+                   "MUSCL-Hancock fallback, HLLC, transmissive boundaries",
+    "vortex32": "isentropic vortex, 32x32 cells, p=3, FV update with limiting, LLF, periodic",
+    "sedov128": "3D Sedov blast, 128^3 cells, p=2, FV update with limiting, HLLC, reflective",
+}
+
+
+def workload_kwargs(name, n_override=None):
+    from spd_gb300 import initial_conditions as ics
+    if name == "quadrant512":
+        n = n_override or 512
+        return dict(p=3, N=(n, n), init_fct=ics.four_quadrant, update="FV", FB=True, riemann_solver_sd="hllc",
+                    riemann_solver_fv="hllc", BC=(("gradfree", "gradfree"),) * 2, cfl_coeff=0.8)
+    if name == "vortex32":
+        n = n_override or 32
+        return dict(p=3, N=(n, n), xlim=(0, 10), ylim=(0, 10), init_fct=ics.isentropic_vortex(), update="FV",
+                    FB=True, riemann_solver_sd="llf", riemann_solver_fv="llf", BC=(("periodic", "periodic"),) * 2)
+    if name == "sedov128":
+        n = n_override or 128
+        return dict(p=2, N=(n, n, n), init_fct=ics.sedov(n), update="FV", FB=True, riemann_solver_sd="hllc",
+                    riemann_solver_fv="hllc", BC=(("reflective", "reflective"),) * 3)
+    raise KeyError(name)
+
+
+def dof_of(kw):
+    cells = 1
+    for n in kw["N"]:
+        cells *= n
+    return cells * (kw["p"] + 1) ** len(kw["N"]), cells
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# roofline bookkeeping
+# ---------------------------------------------------------------------------
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def interior_bytes_per_step(D, p, T, cells):
+    """Compulsory HBM bytes of all k_interior launches of one step (the
+    predictor's fused flux / derivative / Picard kernel), FV update."""
+    n, nf, V = p + 1, p + 2, D + 2
+    NS, NJ = n ** D, n ** (D - 1)
+    u_sp = V * NS * 8
+    u_ader = V * T * NS * 8
+    fi = 2 * D * V * T * NJ * 8
+    tr = 2 * D * V * T * NJ * 8
+    first = u_sp + 2 * D * V * NJ * 8 + u_ader + tr           # it = 0 (one time node)
+    mid = u_ader + u_sp + fi + u_ader + tr                      # 0 < it < m
+    last = u_ader + fi + D * V * T * NJ * nf * 8                # it = m, flux points out
+    return cells * (first + (T - 2) * mid + last), T
+
+
+def fp64_peak_tflops():
+    """cuBLAS FP64 GEMM throughput (burst), the FP64 denominator."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2 * n ** 3 / best / 1e12
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement of the reference's NumPy path
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    workload, n_side, steps, warmup = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path.insert(0, ROOT)
+    import warnings
+    warnings.simplefilter("ignore")
+    import numpy as np
+    from oracle.sdader_oracle import OracleSDADER
+    from spd_gb300.simulator import SDADER_Simulator, initial_state, subcell_faces  # noqa: F401
+    kw = workload_kwargs(workload, n_side)
+    ndim = len(kw["N"])
+    p = kw["p"]
+    ops = SDADER_Simulator.build_operators(p, p)
+    lims = [kw.get(f"{d}lim", (0, 1)) for d in "xyz"[:ndim]]
+    _, W_cv, _, U_sp, U_cv = initial_state(ndim, list(kw["N"]), p, lims, kw["init_fct"], ops, 1.4)
+    state = {"U_sp": U_sp, "U_cv": U_cv, "W_cv": W_cv.copy()}
+    for d in "xyz"[:ndim]:
+        state[f"BC_fp_{d}"] = np.zeros(1)
+        ext = [kw["N"][i] * (p + 1) + 4 for i in range(ndim)]
+        ext["xyz".index(d)] = 2
+        state[f"BC_fv_{d}"] = np.zeros((2, ndim + 2) + tuple(ext[::-1]))
+    o = OracleSDADER(ndim=ndim, N=list(kw["N"]), p=p, m=p, lims=lims, BC=kw["BC"], gamma=1.4,
+                     cfl_coeff=kw.get("cfl_coeff", 0.8), min_c2=1e-10, riemann_solver_sd=kw["riemann_solver_sd"],
+                     riemann_solver_fv=kw["riemann_solver_fv"], slope_limiter="minmod", update=kw["update"],
+                     FB=kw["FB"], tolerance=1e-5, SED=True, NAD="", PAD=True, blending=True, min_rho=1e-10,
+                     max_rho=1e10, min_P=1e-10, godunov=False, ops=ops, state=state)
+    for _ in range(warmup):
+        o.compute_dt()
+        o.perform_update()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.compute_dt()
+        o.perform_update()
+    el = time.perf_counter() - t0
+    dof, _ = dof_of(kw)
+    return dof * steps, el
+
+
+def cpu_baseline(workload, n_side, steps, warmup, procs):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, [(workload, n_side, steps, warmup)] * procs)
+    total_units = sum(r[0] for r in res)
+    tmax = max(r[1] for r in res)
+    return total_units / tmax, tmax
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    n_side = {"quadrant512": 64, "vortex32": 32, "sedov128": 12}[args.workload]
+    steps = max(1, args.steps)
+    value, tmax = cpu_baseline(args.workload, n_side, steps, args.warmup, procs)
+    kw = workload_kwargs(args.workload, n_side)
+    sample = (f"{procs} independent processes, each {args.warmup}+{steps} steps of the same configuration at "
+              f"{'x'.join(str(n) for n in kw['N'])} cells (the full grid needs ~9 GB and ~90 s per step per core)")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": tmax / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOADS[args.workload], "sample_cells": kw["N"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------
+def ours(args):
+    import numpy as np
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from spd_gb300 import SDADER_Simulator
+    kw = workload_kwargs(args.workload)
+    dof, cells = dof_of(kw)
+    s = SDADER_Simulator(verbose=False, **kw)
+    ctx = s._ctx
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    # warm-up
+    for _ in range(args.warmup):
+        s.compute_dt()
+        s.perform_update()
+    torch.cuda.synchronize()
+    ctx.profile_report()
+    launches0 = ctx.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            s.compute_dt()
+            s.perform_update()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ctx.profile(False)
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    launches = ctx.launch_count() - launches0
+    prof = ctx.profile_report()
+    clocks = clk.summary()
+    value = dof * args.steps * world / (ms / 1e3)
+
+    # end to end through the public API with host buffers
+    shape_u = s._shape_of("U_sp")
+    shape_w = s._shape_of("W_cv")
+    U_host = torch.empty(int(np.prod(shape_u)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape_u)
+    W_host = torch.empty(int(np.prod(shape_w)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape_w)
+    U_host[...] = s.dm.U_sp
+    W_host[...] = s.dm.W_cv
+    out = torch.empty(int(np.prod(shape_u)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape_u)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s._ctx.upload("U_sp", U_host)
+        s._ctx.upload("W_cv", W_host)
+        s.compute_dt()
+        s.perform_update()
+        s._ctx.check(s._ctx.lib.spd_download(s._ctx.h, 0, out.ctypes.data_as(
+            __import__("ctypes").POINTER(__import__("ctypes").c_double)), out.size), "download")
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": dof * e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(U_host.nbytes + W_host.nbytes), "d2h_bytes_per_step": int(out.nbytes),
+           "steps": e2e_steps}
+
+    # roofline of the dominant kernel
+    peak_gbs, peak_kind = measured_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 1.0))
+    total_kernel_ms = sum(v[1] for v in prof.values())
+    D, p = len(kw["N"]), kw["p"]
+    roof = None
+    if top[0] == "k_interior":
+        bytes_step, nlaunch_per_step = interior_bytes_per_step(D, p, p + 1, cells)
+        per_launch_bytes = bytes_step / nlaunch_per_step
+        avg_s = top[1][1] / top[1][0] / 1e3
+        achieved = per_launch_bytes / avg_s / 1e9
+        roof = {"bound": "hbm", "kernel": "k_interior", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                "frac": achieved / peak_gbs, "peak_kind": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3}
+    fp64 = None
+    if rank == 0:
+        try:
+            fp64 = fp64_peak_tflops()
+        except Exception:
+            fp64 = None
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            v, tmax = cpu_baseline(args.workload, 128, 1, 0, 1)
+            cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": "1 step of the same configuration at 128x128 cells on one core "
+                             "(CPU restatement of the reference's NumPy path)"}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOADS[args.workload], "cells": cells, "dof": dof,
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2: U_sp alone is "
+                                 f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
+                "roofline": roof,
+                "fp64_gemm_peak_tflops": fp64,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+                "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+                "kernel_share_of_step": total_kernel_ms / ms if ms else None}
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        from spd_gb300.build import build
+        if int(os.environ.get("LOCAL_RANK", "0")) == 0:
+            build()
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

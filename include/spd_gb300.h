@@ -137,6 +137,21 @@ int spd_step(spd_ctx* ctx, int nsteps, double t_end, int mode, double* time_inou
 int spd_end_sim(spd_ctx* ctx);
 /* Wait for all work of the context. */
 int spd_synchronize(spd_ctx* ctx);
+/* Launch subsequent work on an external CUDA stream (a cudaStream_t, for
+ * example the current stream of a framework); NULL restores the context's
+ * own stream.  No reference counterpart (the reference runs on the host or
+ * on CuPy's default stream). */
+int spd_set_stream(spd_ctx* ctx, void* stream);
+/* Per-kernel CUDA-event timing of subsequent launches on the context's
+ * stream (enable = 1) -- the measurement hook of the benchmark; no
+ * reference counterpart (the reference's only timer is the wall clock in
+ * src/sdader_simulator.py:383,387). */
+int spd_profile(spd_ctx* ctx, int enable);
+/* One line "kernel launches total_ms" per kernel recorded since the last
+ * report; clears the record. */
+int spd_profile_report(spd_ctx* ctx, char* buf, size_t len);
+/* Kernels launched by the context since it was created. */
+int spd_launch_count(const spd_ctx* ctx, long long* count);
 int spd_destroy(spd_ctx* ctx);
 const char* spd_last_error(const spd_ctx* ctx);
 const char* spd_version(void);

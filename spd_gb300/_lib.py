@@ -30,6 +30,7 @@ EXPORTS = (
     "spd_create", "spd_upload", "spd_download", "spd_compute_dt", "spd_set_dt",
     "spd_get_dt", "spd_perform_update", "spd_step", "spd_end_sim",
     "spd_synchronize", "spd_destroy", "spd_last_error", "spd_version",
+    "spd_set_stream", "spd_profile", "spd_profile_report", "spd_launch_count",
 )
 
 
@@ -106,6 +107,10 @@ def load():
     lib.spd_synchronize.argtypes = [vp]
     lib.spd_destroy.argtypes = [vp]
     lib.spd_last_error.argtypes = [vp]
+    lib.spd_set_stream.argtypes = [vp, vp]
+    lib.spd_profile.argtypes = [vp, ctypes.c_int]
+    lib.spd_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.spd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.spd_last_error.restype = ctypes.c_char_p
     lib.spd_version.restype = ctypes.c_char_p
     for name in EXPORTS:
@@ -184,6 +189,27 @@ class Context:
 
     def synchronize(self):
         self.check(self.lib.spd_synchronize(self.h), "synchronize")
+
+    def set_stream(self, stream_handle: int | None):
+        self.check(self.lib.spd_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)), "set_stream")
+
+    def profile(self, enable: bool):
+        self.check(self.lib.spd_profile(self.h, int(bool(enable))), "profile")
+
+    def profile_report(self) -> dict:
+        """{kernel: (launches, total_ms)} recorded since the last report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self.check(self.lib.spd_profile_report(self.h, buf, len(buf)), "profile_report")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        self.check(self.lib.spd_launch_count(self.h, ctypes.byref(n)), "launch_count")
+        return n.value
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

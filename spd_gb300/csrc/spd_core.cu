@@ -61,6 +61,16 @@ struct spd_ctx {
   size_t staging_len = 0;
   StepperBase* stepper = nullptr;
   bool fb_ran = false;
+  // stream and launch accounting
+  cudaStream_t own_stream = nullptr;
+  long long launches = 0;
+  bool prof = false;
+  struct Rec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> rec;
+  std::vector<cudaEvent_t> pool;
 };
 
 namespace {
@@ -84,6 +94,39 @@ int fail(spd_ctx* c, int code, const std::string& msg) {
   } while (0)
 
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+cudaEvent_t get_event(spd_ctx* C) {
+  if (!C->pool.empty()) {
+    cudaEvent_t e = C->pool.back();
+    C->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Counts every kernel launch of the context and, while profiling is on,
+// brackets it with CUDA events on the context's stream.
+struct ProfScope {
+  spd_ctx* C;
+  const char* name;
+  cudaEvent_t a = nullptr;
+  ProfScope(spd_ctx* c, const char* n) : C(c), name(n) {
+    ++C->launches;
+    if (C->prof) {
+      a = get_event(C);
+      cudaEventRecord(a, C->stream);
+    }
+  }
+  ~ProfScope() {
+    if (C->prof) {
+      cudaEvent_t b = get_event(C);
+      cudaEventRecord(b, C->stream);
+      C->rec.push_back({name, a, b});
+    }
+  }
+};
 
 template <class T>
 int dalloc(spd_ctx* C, T** p, size_t count) {
@@ -203,8 +246,11 @@ struct Stepper : StepperBase {
 
   int predictor(spd_ctx* C, int final_mode) {
     const Geo& g = C->geo;
-    k_traces_sp<D, P><<<blocks_for(g.Nc, 128), 128, 0, C->stream>>>(C->ops, g, C->U_sp, C->trace[0], C->trace[1],
-                                                                   C->trace[2]);
+    {
+      ProfScope ps_(C, "k_traces_sp");
+      k_traces_sp<D, P><<<blocks_for(g.Nc, 128), 128, 0, C->stream>>>(C->ops, g, C->U_sp, C->trace[0], C->trace[1],
+                                                                     C->trace[2]);
+    }
     CKL();
     const int m = C->T - 1;
     for (int it = 0; it <= m; ++it) {
@@ -212,8 +258,11 @@ struct Stepper : StepperBase {
       const int solver = C->cfg.riemann_solver_sd;
       for (int d = 0; d < D; ++d) {
         const long long tot = (long long)Teff * k::NJ * n_iface(g, d);
-        k_riemann_sd<D, P><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                        C->bcfix[d], C->Fi[d]);
+        {
+          ProfScope ps_(C, "k_riemann_sd");
+          k_riemann_sd<D, P><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
+                                                                          C->bcfix[d], C->Fi[d]);
+        }
         CKL();
       }
       const int mode = (it < m) ? 0 : final_mode;
@@ -221,9 +270,12 @@ struct Stepper : StepperBase {
       const int Tu = (it == 0) ? 1 : C->T;
       dim3 block(cpb, Teff);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
-      k_interior<D, P><<<blocks_for(g.Nc, cpb), block, sm, C->stream>>>(
-          C->ops, g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
-          C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2]);
+      {
+        ProfScope ps_(C, "k_interior");
+        k_interior<D, P><<<blocks_for(g.Nc, cpb), block, sm, C->stream>>>(
+            C->ops, g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
+            C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2]);
+      }
       CKL();
     }
     return 0;
@@ -231,14 +283,20 @@ struct Stepper : StepperBase {
 
   int sp_to_cv(spd_ctx* C) override {
     const Geo& g = C->geo;
-    k_sp_to_cv<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_sp_to_cv, C->U_sp, C->U_cv);
+    {
+      ProfScope ps_(C, "k_sp_to_cv");
+      k_sp_to_cv<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_sp_to_cv, C->U_sp, C->U_cv);
+    }
     CKL();
     return 0;
   }
 
   int wcv(spd_ctx* C) override {
     const Geo& g = C->geo;
-    k_prim_only<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->U_cv, C->W_cv);
+    {
+      ProfScope ps_(C, "k_prim_only");
+      k_prim_only<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->U_cv, C->W_cv);
+    }
     CKL();
     return 0;
   }
@@ -247,9 +305,15 @@ struct Stepper : StepperBase {
     const Geo& g = C->geo;
     CK(cudaMemsetAsync(C->flags + 1, 0, sizeof(int), C->stream));
     CK(cudaMemsetAsync(C->counts + 2, 0, sizeof(unsigned long long), C->stream));
-    k_cmax_only<D, P><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->W_cv, C->counts + 2, C->flags + 1);
+    {
+      ProfScope ps_(C, "k_cmax_only");
+      k_cmax_only<D, P><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->W_cv, C->counts + 2, C->flags + 1);
+    }
     CKL();
-    k_dt_final<<<1, 1, 0, C->stream>>>(C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1, C->dt);
+    {
+      ProfScope ps_(C, "k_dt_final");
+      k_dt_final<<<1, 1, 0, C->stream>>>(C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1, C->dt);
+    }
     CKL();
     return 0;
   }
@@ -260,8 +324,11 @@ struct Stepper : StepperBase {
     // switch_to_finite_volume (src/sdader_simulator.py:288-298)
     if (int r = sp_to_cv(C)) return r;
     for (int d = 0; d < D; ++d) {
-      k_integrate_faces<D, P><<<blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->stream>>>(C->ops, g, d, C->Ffp[d],
-                                                                                          C->F_HO[d]);
+      {
+        ProfScope ps_(C, "k_integrate_faces");
+        k_integrate_faces<D, P><<<blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->stream>>>(C->ops, g, d, C->Ffp[d],
+                                                                                            C->F_HO[d]);
+      }
       CKL();
     }
     long long nface[3] = {1, 1, 1};
@@ -270,9 +337,12 @@ struct Stepper : StepperBase {
       const double w_i = C->ops.w_tp[i];
       const double* FH[3] = {nullptr, nullptr, nullptr};
       for (int d = 0; d < D; ++d) FH[d] = C->F_HO[d] + (long long)i * k::V * nface[d];
-      k_fv_candidate<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, C->dt, w_i, FH[0], FH[1], FH[2],
-                                                                     C->U_cv, C->U_new, C->ext_old, C->ext_new,
-                                                                     cf.FB ? 1 : 0);
+      {
+        ProfScope ps_(C, "k_fv_candidate");
+        k_fv_candidate<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, C->dt, w_i, FH[0], FH[1], FH[2],
+                                                                       C->U_cv, C->U_new, C->ext_old, C->ext_new,
+                                                                       cf.FB ? 1 : 0);
+      }
       CKL();
       if (cf.FB) {
         // detect_troubles (src/trouble_detection.py:5-87)
@@ -280,8 +350,11 @@ struct Stepper : StepperBase {
           if (int r = ghost(C, d, 1, k::V, C->ext_old, nullptr)) return r;
         }
         CK(cudaMemsetAsync(C->flags, 0, sizeof(int), C->stream));
-        k_nad<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, cf.tolerance, cf.NAD_delta, P > 0 ? 1 : 0, C->ext_old,
-                                                             C->ext_new, C->mask, C->flags);
+        {
+          ProfScope ps_(C, "k_nad");
+          k_nad<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, cf.tolerance, cf.NAD_delta, P > 0 ? 1 : 0, C->ext_old,
+                                                               C->ext_new, C->mask, C->flags);
+        }
         CKL();
         const int sed = (P > 1 && cf.SED) ? 1 : 0;
         if (sed) {
@@ -289,21 +362,30 @@ struct Stepper : StepperBase {
             if (int r = ghost(C, d, 1, k::V, C->ext_new, C->flags)) return r;
           }
         }
-        k_troubles<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, sed, cf.PAD, cf.min_rho, cf.max_rho,
-                                                                  cf.min_P, C->mask, C->flags, C->ext_new,
-                                                                  C->theta_src, C->troubles);
+        {
+          ProfScope ps_(C, "k_troubles");
+          k_troubles<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, sed, cf.PAD, cf.min_rho, cf.max_rho,
+                                                                    cf.min_P, C->mask, C->flags, C->ext_new,
+                                                                    C->theta_src, C->troubles);
+        }
         CKL();
         for (int d = 0; d < D; ++d) {
           if (int r = ghost(C, d, 0, 1, C->theta_src, nullptr)) return r;
         }
         double* th = C->theta_src;
         if (cf.blending) {
-          k_blend_neighbours<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, C->theta_src, C->theta_a);
+          {
+            ProfScope ps_(C, "k_blend_neighbours");
+            k_blend_neighbours<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, C->theta_src, C->theta_a);
+          }
           CKL();
           double* in = C->theta_a;
           double* out = C->theta_b;
           for (int d = 0; d < D; ++d) {
-            k_blend_last<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, d, in, out);
+            {
+              ProfScope ps_(C, "k_blend_last");
+              k_blend_last<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, d, in, out);
+            }
             CKL();
             std::swap(in, out);
           }
@@ -315,19 +397,31 @@ struct Stepper : StepperBase {
         CK(cudaMemsetAsync(C->mark_q, 0, (size_t)g.Nq, C->stream));
         CK(cudaMemsetAsync(C->counts, 0, 2 * sizeof(unsigned long long), C->stream));
         for (int d = 0; d < D; ++d) {
-          k_affected<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.godunov, th, C->aff[d],
-                                                                        C->mark_cell, C->mark_q, C->flags + 2);
+          {
+            ProfScope ps_(C, "k_affected");
+            k_affected<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.godunov, th, C->aff[d],
+                                                                          C->mark_cell, C->mark_q, C->flags + 2);
+          }
           CKL();
         }
-        k_compact<<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g.Nqe, C->mark_cell, C->list_cell, C->counts);
+        {
+          ProfScope ps_(C, "k_compact");
+          k_compact<<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g.Nqe, C->mark_cell, C->list_cell, C->counts);
+        }
         CKL();
-        k_compact<<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g.Nq, C->mark_q, C->list_q, C->counts + 1);
+        {
+          ProfScope ps_(C, "k_compact");
+          k_compact<<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g.Nq, C->mark_q, C->list_q, C->counts + 1);
+        }
         CKL();
         k_muscl_cells_grid(C, w_i);
         CKL();
         for (int d = 0; d < D; ++d) {
-          k_muscl_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, cf.godunov,
-                                                                           C->aff[d], C->Mpred, C->S, C->F_FB[d]);
+          {
+            ProfScope ps_(C, "k_muscl_faces");
+            k_muscl_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, cf.godunov,
+                                                                             C->aff[d], C->Mpred, C->S, C->F_FB[d]);
+          }
           CKL();
         }
         k_fv_correct_grid(C, w_i, FH);
@@ -337,7 +431,10 @@ struct Stepper : StepperBase {
       std::swap(C->U_cv, C->U_new);
     }
     // switch_to_high_order (src/sdader_simulator.py:300-307)
-    k_cv_to_sp<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_cv_to_sp, C->U_cv, C->U_sp);
+    {
+      ProfScope ps_(C, "k_cv_to_sp");
+      k_cv_to_sp<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_cv_to_sp, C->U_cv, C->U_sp);
+    }
     CKL();
     return 0;
   }
@@ -345,17 +442,23 @@ struct Stepper : StepperBase {
   void k_muscl_cells_grid(spd_ctx* C, double w_i) {
     const Geo& g = C->geo;
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nqe, 128));
-    k_muscl_cells<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i, C->list_cell,
-                                                          C->counts, C->ext_old, C->Mpred, C->S);
+    {
+      ProfScope ps_(C, "k_muscl_cells");
+      k_muscl_cells<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i, C->list_cell,
+                                                            C->counts, C->ext_old, C->Mpred, C->S);
+    }
   }
 
   void k_fv_correct_grid(spd_ctx* C, double w_i, const double* const* FH) {
     const Geo& g = C->geo;
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nq, 128));
-    k_fv_correct<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->dt, w_i, C->cfg.godunov, C->list_q,
-                                                         C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
-                                                         C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv,
-                                                         C->U_new);
+    {
+      ProfScope ps_(C, "k_fv_correct");
+      k_fv_correct<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->dt, w_i, C->cfg.godunov, C->list_q,
+                                                           C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
+                                                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv,
+                                                           C->U_new);
+    }
   }
 
   int ghost(spd_ctx* C, int d, int all, int nv, double* ext, const int* gate) {
@@ -363,7 +466,10 @@ struct Stepper : StepperBase {
     const int o0 = (d == 0) ? 1 : 0;
     const int o1 = (d == 2) ? 1 : 2;
     const long long tot = 2LL * nv * NGH * g.Xe[o0] * g.Xe[o1];
-    k_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, all, nv, k::V, ext, C->bcbuf[d], gate);
+    {
+      ProfScope ps_(C, "k_ghost");
+      k_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, all, nv, k::V, ext, C->bcbuf[d], gate);
+    }
     CKL();
     return 0;
   }
@@ -510,7 +616,8 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   std::memcpy(C->ops.invader, ops->invader, sizeof(double) * T * T);
   std::memcpy(C->ops.w_tp, ops->w_tp, sizeof(double) * T);
 
-  CK(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&C->own_stream, cudaStreamNonBlocking));
+  C->stream = C->own_stream;
 
   // whole-cell operator products ((A*A)*A) for sp_to_cv and cv_to_sp
   {
@@ -626,9 +733,65 @@ int spd_destroy(spd_ctx* C) {
   if (!C) return SPD_ERR_ARG;
   if (C->stream) cudaStreamSynchronize(C->stream);
   for (void* p : C->allocs) cudaFree(p);
-  if (C->stream) cudaStreamDestroy(C->stream);
+  for (auto& r : C->rec) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : C->pool) cudaEventDestroy(e);
+  if (C->own_stream) cudaStreamDestroy(C->own_stream);
   delete C->stepper;
   delete C;
+  return SPD_OK;
+}
+
+int spd_set_stream(spd_ctx* C, void* stream) {
+  if (!C) return SPD_ERR_ARG;
+  CK(cudaStreamSynchronize(C->stream));
+  C->stream = stream ? static_cast<cudaStream_t>(stream) : C->own_stream;
+  return SPD_OK;
+}
+
+int spd_profile(spd_ctx* C, int enable) {
+  if (!C) return SPD_ERR_ARG;
+  C->prof = enable != 0;
+  return SPD_OK;
+}
+
+int spd_profile_report(spd_ctx* C, char* buf, size_t len) {
+  if (!C || !buf || len == 0) return SPD_ERR_ARG;
+  CK(cudaStreamSynchronize(C->stream));
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<long long> cnt;
+  for (auto& r : C->rec) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    size_t k = 0;
+    while (k < names.size() && names[k] != r.name) ++k;
+    if (k == names.size()) {
+      names.push_back(r.name);
+      ms.push_back(0.0);
+      cnt.push_back(0);
+    }
+    ms[k] += t;
+    cnt[k] += 1;
+    C->pool.push_back(r.a);
+    C->pool.push_back(r.b);
+  }
+  C->rec.clear();
+  std::string out;
+  char line[256];
+  for (size_t k = 0; k < names.size(); ++k) {
+    std::snprintf(line, sizeof(line), "%s %lld %.6f\n", names[k].c_str(), cnt[k], ms[k]);
+    out += line;
+  }
+  std::snprintf(buf, len, "%s", out.c_str());
+  return out.size() + 1 > len ? fail(C, SPD_ERR_ARG, "profile report truncated") : SPD_OK;
+}
+
+int spd_launch_count(const spd_ctx* C, long long* count) {
+  if (!C || !count) return SPD_ERR_ARG;
+  *count = C->launches;
   return SPD_OK;
 }
 
