@@ -248,7 +248,7 @@ def ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from spd_gb300 import SDADER_Simulator
-    kw = workload_kwargs(args.workload)
+    kw = workload_kwargs(args.workload, args.cells)
     dof, cells = dof_of(kw)
     s = SDADER_Simulator(verbose=False, **kw)
     ctx = s._ctx
@@ -339,7 +339,9 @@ def ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOADS[args.workload], "cells": cells, "dof": dof,
+                "config": {"workload": WORKLOADS[args.workload] + (f" (reduced to {args.cells} cells per side)"
+                                                                   if args.cells else ""),
+                           "cells": cells, "dof": dof,
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2: U_sp alone is "
                                  f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
@@ -362,6 +364,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=None,
+                    help="cells per direction (a smaller case of the workload, for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -1,0 +1,160 @@
+// Host-side context of the C ABI (include/spd_gb300.h) shared by the
+// translation units of the library: the spd_ctx struct, launch accounting
+// and the per-(D,P) stepper interface.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/spd_gb300.h"
+#include "spd_fv.cuh"
+
+namespace spd_host {
+struct StepperBase;
+}
+
+struct spd_ctx {
+  spd_config cfg{};
+  spd::Ops ops{};
+  spd::Geo geo{};
+  spd::FvGeo fvg{};
+  int D = 0, P = 0, n = 0, nf = 0, T = 0, V = 0, NS = 0, NJ = 0;
+  double h_dt = 0.0;  // h_min / (p+1)
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<void*> allocs;
+  // state
+  double *U_sp = nullptr, *U_cv = nullptr, *W_cv = nullptr, *U_new = nullptr;
+  double* dt = nullptr;
+  // predictor scratch
+  double* U_ader = nullptr;
+  double* trace[3] = {nullptr, nullptr, nullptr};
+  double* Fi[3] = {nullptr, nullptr, nullptr};
+  double* Ffp[3] = {nullptr, nullptr, nullptr};
+  double* bcfix[3] = {nullptr, nullptr, nullptr};
+  // FV scratch
+  double* F_HO[3] = {nullptr, nullptr, nullptr};
+  double *ext_old = nullptr, *ext_new = nullptr, *theta_src = nullptr, *theta_a = nullptr, *theta_b = nullptr;
+  double* theta_final = nullptr;
+  double* bcbuf[3] = {nullptr, nullptr, nullptr};
+  unsigned char *mask = nullptr, *mark_cell = nullptr, *mark_q = nullptr;
+  int* flags = nullptr;  // [0] any possible trouble, [1] nan in cmax, [2] marked faces
+  unsigned long long* counts = nullptr;  // [0] cells, [1] subcells, [2] cmax bits
+  long long *list_cell = nullptr, *list_q = nullptr;
+  double* troubles = nullptr;
+  double* aff[3] = {nullptr, nullptr, nullptr};
+  double* F_FB[3] = {nullptr, nullptr, nullptr};
+  double *Mpred = nullptr, *S = nullptr;
+  double *K_sp_to_cv = nullptr, *K_cv_to_sp = nullptr;
+  double* geo_arrays = nullptr;
+  double* staging = nullptr;
+  size_t staging_len = 0;
+  spd_host::StepperBase* stepper = nullptr;
+  bool fb_ran = false;
+  // stream and launch accounting
+  cudaStream_t own_stream = nullptr;
+  long long launches = 0;
+  bool prof = false;
+  struct Rec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> rec;
+  std::vector<cudaEvent_t> pool;
+};
+
+namespace spd_host {
+using namespace spd;
+
+inline int fail(spd_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return fail(C, SPD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+#define CKL()                                                                                       \
+  do {                                                                                              \
+    cudaError_t e_ = cudaGetLastError();                                                            \
+    if (e_ != cudaSuccess) return fail(C, SPD_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+inline cudaEvent_t get_event(spd_ctx* C) {
+  if (!C->pool.empty()) {
+    cudaEvent_t e = C->pool.back();
+    C->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Counts every kernel launch of the context and, while profiling is on,
+// brackets it with CUDA events on the context's stream.
+struct ProfScope {
+  spd_ctx* C;
+  const char* name;
+  cudaEvent_t a = nullptr;
+  ProfScope(spd_ctx* c, const char* n) : C(c), name(n) {
+    ++C->launches;
+    if (C->prof) {
+      a = get_event(C);
+      cudaEventRecord(a, C->stream);
+    }
+  }
+  ~ProfScope() {
+    if (C->prof) {
+      cudaEvent_t b = get_event(C);
+      cudaEventRecord(b, C->stream);
+      C->rec.push_back({name, a, b});
+    }
+  }
+};
+
+template <class T>
+int dalloc(spd_ctx* C, T** p, size_t count) {
+  void* ptr = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+  if (e != cudaSuccess) return fail(C, SPD_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  C->allocs.push_back(ptr);
+  *p = static_cast<T*>(ptr);
+  return 0;
+}
+
+
+// --------------------------------------------------------------------------
+// per-(D,P) launch sequence
+// --------------------------------------------------------------------------
+struct StepperBase {
+  virtual ~StepperBase() {}
+  virtual int update(spd_ctx* C) = 0;    // perform_update with the current dt
+  virtual int wcv(spd_ctx* C) = 0;       // W_cv = prim(U_cv)
+  virtual int cmax(spd_ctx* C) = 0;      // dt from W_cv
+  virtual int sp_to_cv(spd_ctx* C) = 0;  // U_cv = sp_to_cv(U_sp)
+  virtual int configure(spd_ctx* C) = 0;
+  int cpb = 32;
+  size_t smem = 0;
+};
+
+constexpr int BS = 256;
+constexpr int PERSIST_BLOCKS = 152 * 8;
+
+StepperBase* make_stepper_d1(int P);
+StepperBase* make_stepper_d2(int P);
+StepperBase* make_stepper_d3(int P);
+
+}  // namespace spd_host

@@ -412,7 +412,7 @@ __global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__
 
 // compaction of marked indices by warp ballot: writes the marked indices
 // into list and their count into *count.
-__global__ void k_compact(long long total, const unsigned char* __restrict__ mark, long long* __restrict__ list,
+static __global__ void k_compact(long long total, const unsigned char* __restrict__ mark, long long* __restrict__ list,
                           unsigned long long* __restrict__ count) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const bool m = (i < total) && mark[i];
@@ -589,7 +589,7 @@ __global__ void k_wcv_cmax(Geo g, const double* __restrict__ U_cv, double* __res
   }
 }
 
-__global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
+static __global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
                            double* dt) {
   const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
                                 : __longlong_as_double((long long)*cmax_bits);

@@ -33,6 +33,8 @@ struct Geo {
   long long Nq;    // subcells
   long long Nqe;   // extended subcells
   double h[3];
+  double inv_h[3];  // 1/h, used only when h is a power of two (then x/h == x*(1/h) exactly)
+  int h_pow2[3];
   double gamma, min_c2;
   int bc[3][2];
 };
@@ -256,12 +258,14 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
             for (int f = 0; f < k::nf; ++f)
               Ffp[d][((((long long)v * g.T + tl) * k::NJ + j) * k::nf + f) * g.Nc + c] = Fl[v][f];
         } else {
-          const double hd = g.h[d];
+          const double hd = g.h[d], ihd = g.inv_h[d];
+          const bool pow2 = g.h_pow2[d] != 0;
 #pragma unroll
           for (int v = 0; v < k::V; ++v) {
 #pragma unroll
             for (int so = 0; so < k::n; ++so) {
-              const double val = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d) / hd;
+              const double dsum = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d);
+              const double val = pow2 ? dsum * ihd : dsum / hd;
               const int s = sp_index<D, P>(d, j, so);
               double* slot = &dudt_s[(((long long)v * k::NS + s) * Teff + tl) * CPB + cl];
               *slot = (d == 0) ? val : *slot + val;

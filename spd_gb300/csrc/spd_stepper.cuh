@@ -1,0 +1,314 @@
+// Launch sequence of one SD-ADER step for dimension D and degree P
+// (src/sdader_simulator.py:361-378); instantiated per dimension in
+// spd_step_d1.cu, spd_step_d2.cu and spd_step_d3.cu.
+#pragma once
+#include "spd_ctx.cuh"
+
+namespace spd_host {
+
+template <int D, int P>
+__global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned long long* __restrict__ cmax_bits,
+                            int* __restrict__ nan_flag) {
+  constexpr int P_ = D + 1;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double cval = 0.0;
+  bool isnan_c = false;
+  if (q < g.Nq) {
+    double c = sound_speed(W_cv[(long long)P_ * g.Nq + q], W_cv[q], g.gamma, g.min_c2) * (double)D;
+#pragma unroll
+    for (int v = 1; v <= D; ++v) c = c + fabs(W_cv[(long long)v * g.Nq + q]);
+    if (c != c) isnan_c = true;
+    else cval = c;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, cval, off);
+    cval = (o > cval) ? o : cval;
+  }
+  const unsigned nb = __ballot_sync(0xffffffffu, isnan_c);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(cmax_bits, (unsigned long long)__double_as_longlong(cval));
+    if (nb) atomicOr(nan_flag, 1);
+  }
+}
+
+template <int D>
+__global__ void k_prim_only(Geo g, const double* __restrict__ U_cv, double* __restrict__ W_cv) {
+  constexpr int V = D + 2;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= g.Nq) return;
+  double u[V], W[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
+  prim<D>(u, W, g.gamma, 0);
+#pragma unroll
+  for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
+}
+
+
+template <int D, int P>
+struct Stepper : StepperBase {
+  using k = K<D, P>;
+
+  int configure(spd_ctx* C) override {
+    // cells per block of the interior kernel: bounded by 200 KB of shared memory
+    const size_t per_cell = (size_t)k::V * k::NS * C->T * sizeof(double);
+    cpb = 32;
+    while (cpb > 1 && per_cell * cpb > 200 * 1024) cpb /= 2;
+    smem = per_cell * cpb;
+    CK(cudaFuncSetAttribute(k_interior<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+  }
+
+  int predictor(spd_ctx* C, int final_mode) {
+    const Geo& g = C->geo;
+    {
+      ProfScope ps_(C, "k_traces_sp");
+      k_traces_sp<D, P><<<blocks_for(g.Nc, 128), 128, 0, C->stream>>>(C->ops, g, C->U_sp, C->trace[0], C->trace[1],
+                                                                     C->trace[2]);
+    }
+    CKL();
+    const int m = C->T - 1;
+    for (int it = 0; it <= m; ++it) {
+      const int Teff = (it == 0) ? 1 : C->T;
+      const int solver = C->cfg.riemann_solver_sd;
+      for (int d = 0; d < D; ++d) {
+        const long long tot = (long long)Teff * k::NJ * n_iface(g, d);
+        {
+          ProfScope ps_(C, "k_riemann_sd");
+          k_riemann_sd<D, P><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
+                                                                          C->bcfix[d], C->Fi[d]);
+        }
+        CKL();
+      }
+      const int mode = (it < m) ? 0 : final_mode;
+      const double* Uin = (it == 0) ? C->U_sp : C->U_ader;
+      const int Tu = (it == 0) ? 1 : C->T;
+      dim3 block(cpb, Teff);
+      const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
+      {
+        ProfScope ps_(C, "k_interior");
+        k_interior<D, P><<<blocks_for(g.Nc, cpb), block, sm, C->stream>>>(
+            C->ops, g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
+            C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2]);
+      }
+      CKL();
+    }
+    return 0;
+  }
+
+  int sp_to_cv(spd_ctx* C) override {
+    const Geo& g = C->geo;
+    {
+      ProfScope ps_(C, "k_sp_to_cv");
+      k_sp_to_cv<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_sp_to_cv, C->U_sp, C->U_cv);
+    }
+    CKL();
+    return 0;
+  }
+
+  int wcv(spd_ctx* C) override {
+    const Geo& g = C->geo;
+    {
+      ProfScope ps_(C, "k_prim_only");
+      k_prim_only<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->U_cv, C->W_cv);
+    }
+    CKL();
+    return 0;
+  }
+
+  int cmax(spd_ctx* C) override {
+    const Geo& g = C->geo;
+    CK(cudaMemsetAsync(C->flags + 1, 0, sizeof(int), C->stream));
+    CK(cudaMemsetAsync(C->counts + 2, 0, sizeof(unsigned long long), C->stream));
+    {
+      ProfScope ps_(C, "k_cmax_only");
+      k_cmax_only<D, P><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->W_cv, C->counts + 2, C->flags + 1);
+    }
+    CKL();
+    {
+      ProfScope ps_(C, "k_dt_final");
+      k_dt_final<<<1, 1, 0, C->stream>>>(C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1, C->dt);
+    }
+    CKL();
+    return 0;
+  }
+
+  int fv_update(spd_ctx* C) {
+    const Geo& g = C->geo;
+    const spd_config& cf = C->cfg;
+    // switch_to_finite_volume (src/sdader_simulator.py:288-298)
+    if (int r = sp_to_cv(C)) return r;
+    for (int d = 0; d < D; ++d) {
+      {
+        ProfScope ps_(C, "k_integrate_faces");
+        k_integrate_faces<D, P><<<blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->stream>>>(C->ops, g, d, C->Ffp[d],
+                                                                                            C->F_HO[d]);
+      }
+      CKL();
+    }
+    long long nface[3] = {1, 1, 1};
+    for (int d = 0; d < D; ++d) nface[d] = n_faces(g, d);
+    for (int i = 0; i < C->T; ++i) {
+      const double w_i = C->ops.w_tp[i];
+      const double* FH[3] = {nullptr, nullptr, nullptr};
+      for (int d = 0; d < D; ++d) FH[d] = C->F_HO[d] + (long long)i * k::V * nface[d];
+      {
+        ProfScope ps_(C, "k_fv_candidate");
+        k_fv_candidate<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, C->dt, w_i, FH[0], FH[1], FH[2],
+                                                                       C->U_cv, C->U_new, C->ext_old, C->ext_new,
+                                                                       cf.FB ? 1 : 0);
+      }
+      CKL();
+      if (cf.FB) {
+        // detect_troubles (src/trouble_detection.py:5-87)
+        for (int d = 0; d < D; ++d) {
+          if (int r = ghost(C, d, 1, k::V, C->ext_old, nullptr)) return r;
+        }
+        CK(cudaMemsetAsync(C->flags, 0, sizeof(int), C->stream));
+        {
+          ProfScope ps_(C, "k_nad");
+          k_nad<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, cf.tolerance, cf.NAD_delta, P > 0 ? 1 : 0, C->ext_old,
+                                                               C->ext_new, C->mask, C->flags);
+        }
+        CKL();
+        const int sed = (P > 1 && cf.SED) ? 1 : 0;
+        if (sed) {
+          for (int d = 0; d < D; ++d) {
+            if (int r = ghost(C, d, 1, k::V, C->ext_new, C->flags)) return r;
+          }
+        }
+        {
+          ProfScope ps_(C, "k_troubles");
+          k_troubles<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, sed, cf.PAD, cf.min_rho, cf.max_rho,
+                                                                    cf.min_P, C->mask, C->flags, C->ext_new,
+                                                                    C->theta_src, C->troubles);
+        }
+        CKL();
+        for (int d = 0; d < D; ++d) {
+          if (int r = ghost(C, d, 0, 1, C->theta_src, nullptr)) return r;
+        }
+        double* th = C->theta_src;
+        if (cf.blending) {
+          {
+            ProfScope ps_(C, "k_blend_neighbours");
+            k_blend_neighbours<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, C->theta_src, C->theta_a);
+          }
+          CKL();
+          double* in = C->theta_a;
+          double* out = C->theta_b;
+          for (int d = 0; d < D; ++d) {
+            {
+              ProfScope ps_(C, "k_blend_last");
+              k_blend_last<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, d, in, out);
+            }
+            CKL();
+            std::swap(in, out);
+          }
+          th = in;
+        }
+        C->theta_final = th;
+        // affected faces, marks and the fallback fluxes (src/sdader_simulator.py:343-346)
+        CK(cudaMemsetAsync(C->mark_cell, 0, (size_t)g.Nqe, C->stream));
+        CK(cudaMemsetAsync(C->mark_q, 0, (size_t)g.Nq, C->stream));
+        CK(cudaMemsetAsync(C->counts, 0, 2 * sizeof(unsigned long long), C->stream));
+        for (int d = 0; d < D; ++d) {
+          {
+            ProfScope ps_(C, "k_affected");
+            k_affected<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.godunov, th, C->aff[d],
+                                                                          C->mark_cell, C->mark_q, C->flags + 2);
+          }
+          CKL();
+        }
+        {
+          ProfScope ps_(C, "k_compact");
+          k_compact<<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g.Nqe, C->mark_cell, C->list_cell, C->counts);
+        }
+        CKL();
+        {
+          ProfScope ps_(C, "k_compact");
+          k_compact<<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g.Nq, C->mark_q, C->list_q, C->counts + 1);
+        }
+        CKL();
+        k_muscl_cells_grid(C, w_i);
+        CKL();
+        for (int d = 0; d < D; ++d) {
+          {
+            ProfScope ps_(C, "k_muscl_faces");
+            k_muscl_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, cf.godunov,
+                                                                             C->aff[d], C->Mpred, C->S, C->F_FB[d]);
+          }
+          CKL();
+        }
+        k_fv_correct_grid(C, w_i, FH);
+        CKL();
+        C->fb_ran = true;
+      }
+      std::swap(C->U_cv, C->U_new);
+    }
+    // switch_to_high_order (src/sdader_simulator.py:300-307)
+    {
+      ProfScope ps_(C, "k_cv_to_sp");
+      k_cv_to_sp<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_cv_to_sp, C->U_cv, C->U_sp);
+    }
+    CKL();
+    return 0;
+  }
+
+  void k_muscl_cells_grid(spd_ctx* C, double w_i) {
+    const Geo& g = C->geo;
+    const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nqe, 128));
+    {
+      ProfScope ps_(C, "k_muscl_cells");
+      k_muscl_cells<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i, C->list_cell,
+                                                            C->counts, C->ext_old, C->Mpred, C->S);
+    }
+  }
+
+  void k_fv_correct_grid(spd_ctx* C, double w_i, const double* const* FH) {
+    const Geo& g = C->geo;
+    const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nq, 128));
+    {
+      ProfScope ps_(C, "k_fv_correct");
+      k_fv_correct<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->dt, w_i, C->cfg.godunov, C->list_q,
+                                                           C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
+                                                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv,
+                                                           C->U_new);
+    }
+  }
+
+  int ghost(spd_ctx* C, int d, int all, int nv, double* ext, const int* gate) {
+    const Geo& g = C->geo;
+    const int o0 = (d == 0) ? 1 : 0;
+    const int o1 = (d == 2) ? 1 : 2;
+    const long long tot = 2LL * nv * NGH * g.Xe[o0] * g.Xe[o1];
+    {
+      ProfScope ps_(C, "k_ghost");
+      k_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, all, nv, k::V, ext, C->bcbuf[d], gate);
+    }
+    CKL();
+    return 0;
+  }
+
+  int update(spd_ctx* C) override {
+    const int final_mode = (C->cfg.update == SPD_UPDATE_SD) ? 1 : 2;
+    if (int r = predictor(C, final_mode)) return r;
+    if (C->cfg.update == SPD_UPDATE_FV) {
+      if (int r = fv_update(C)) return r;
+    }
+    // W_cv = prim(U_cv) (src/sdader_simulator.py:376)
+    return wcv(C);
+  }
+};
+
+template <int D>
+StepperBase* make_stepper_for(int P) {
+  switch (P) {
+    case 1: return new Stepper<D, 1>();
+    case 2: return new Stepper<D, 2>();
+    case 3: return new Stepper<D, 3>();
+    case 4: return new Stepper<D, 4>();
+    default: return nullptr;
+  }
+}
+
+}  // namespace spd_host
