@@ -153,6 +153,21 @@ int spd_profile_report(spd_ctx* ctx, char* buf, size_t len);
 /* Kernels launched by the context since it was created. */
 int spd_launch_count(const spd_ctx* ctx, long long* count);
 int spd_destroy(spd_ctx* ctx);
+/* CFL time step dt = cfl_coeff * (h / max(ndim*c_s + sum |v|)) from
+ * primitive subcell averages already on the device, without allocating
+ * device memory.  No counterpart in the reference: it serves callers that
+ * must not call cudaMalloc (graph capture, a framework allocator that owns
+ * device memory, allocation-free real-time loops).  W_cv_dev holds
+ * ndim + 2 variables one after the other, n_subcells values each (any
+ * subcell order); h = h_min / (p + 1); dt_dev receives one double; the
+ * work is queued on ``stream`` (a cudaStream_t, NULL = default stream).
+ * At most 4,194,304 subcells per call (larger returns SPD_ERR_ARG).  Its
+ * scratch is a fixed 128 KB array in the library image: the first call on
+ * each device looks up that array's device address (make the first call
+ * before any stream capture); calls that overlap on the GPU share the
+ * array and race. */
+int spd_cfl_dt_noalloc(const double* W_cv_dev, long long n_subcells, int ndim, double gamma, double min_c2,
+                       double cfl_coeff, double h, double* dt_dev, void* stream);
 const char* spd_last_error(const spd_ctx* ctx);
 const char* spd_version(void);
 
