@@ -153,6 +153,12 @@ int spd_profile_report(spd_ctx* ctx, char* buf, size_t len);
 /* Kernels launched by the context since it was created. */
 int spd_launch_count(const spd_ctx* ctx, long long* count);
 int spd_destroy(spd_ctx* ctx);
+/* Diagnostic: multiplies n generated operand pairs (all exponent ranges,
+ * ties, sticky patterns, zeros, subnormals, infinities, NaNs) with the
+ * kernels' integer-pipe binary64 multiply and with the FP64 unit, and
+ * returns the number of results whose bits differ (expected 0).  No
+ * reference counterpart. */
+int spd_selftest_fp64(long long n, unsigned long long seed, unsigned long long* mismatches_out);
 /* CFL time step dt = cfl_coeff * (h / max(ndim*c_s + sum |v|)) from
  * primitive subcell averages already on the device, without allocating
  * device memory.  No counterpart in the reference: it serves callers that

@@ -8,7 +8,19 @@
 #include <cstdint>
 #include <cmath>
 
+#include "spd_emul.cuh"
+
 namespace spd {
+
+// Product used by the contractions: the integer-pipe multiply (same bits as
+// the FP64 unit, see spd_emul.cuh) unless SPD_NATIVE_MUL is defined.
+__device__ __forceinline__ double mulx(double a, double b) {
+#ifdef SPD_NATIVE_MUL
+  return a * b;
+#else
+  return emul_mul(a, b);
+#endif
+}
 
 constexpr int MAXN = 5;   // p <= 4
 constexpr int MAXNF = 6;
@@ -188,20 +200,20 @@ __device__ __forceinline__ void riemann(int solver, const double* ML, const doub
 // (src/transforms.py:3-25).
 template <int L>
 __device__ __forceinline__ double dot_seq(const double* A, const double* x) {
-  double acc = A[0] * x[0];
+  double acc = mulx(A[0], x[0]);
 #pragma unroll
-  for (int s = 1; s < L; ++s) acc = acc + A[s] * x[s];
+  for (int s = 1; s < L; ++s) acc = acc + mulx(A[s], x[s]);
   return acc;
 }
 template <int L>
 __device__ __forceinline__ double dot_lanes2(const double* A, const double* x) {
-  double e = A[0] * x[0];
+  double e = mulx(A[0], x[0]);
   if (L == 1) return e;
-  double o = A[1] * x[1];
+  double o = mulx(A[1], x[1]);
 #pragma unroll
   for (int s = 2; s < L; ++s) {
-    if (s % 2 == 0) e = e + A[s] * x[s];
-    else o = o + A[s] * x[s];
+    if (s % 2 == 0) e = e + mulx(A[s], x[s]);
+    else o = o + mulx(A[s], x[s]);
   }
   return e + o;
 }
