@@ -252,6 +252,8 @@ def ours(args):
     dof, cells = dof_of(kw)
     s = SDADER_Simulator(verbose=False, **kw)
     ctx = s._ctx
+    if args.mul_stride is not None:
+        ctx.set_mul_stride(args.mul_stride)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     # warm-up
@@ -364,6 +366,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mul-stride", type=int, default=None,
+                    help="every k-th contraction product on the integer pipes (0 none, 1 all)")
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per direction (a smaller case of the workload, for profiling)")
     args = ap.parse_args()

@@ -35,6 +35,7 @@ extern "C" {
 #endif
 
 typedef struct spd_ctx spd_ctx;
+typedef struct spd_ensemble spd_ensemble;
 
 enum spd_status {
   SPD_OK = 0,
@@ -176,6 +177,33 @@ int spd_cfl_dt_noalloc(const double* W_cv_dev, long long n_subcells, int ndim, d
                        double cfl_coeff, double h, double* dt_dev, void* stream);
 const char* spd_last_error(const spd_ctx* ctx);
 const char* spd_version(void);
+
+/* ---- batched ensembles (no reference counterpart) ----------------------
+ * Many independent contexts of different sizes advanced together: the step
+ * of every instance (its own CFL dt, predictor, FV update and a device-side
+ * time accumulator) is recorded once into one CUDA graph whose branches run
+ * on ``nstreams`` streams (instances assigned largest-first to the least
+ * loaded stream); one launch advances every instance ``steps_per_launch``
+ * steps.  The contexts stay owned by the caller and must outlive the
+ * ensemble; their simulated time restarts at 0 in the device accumulator. */
+int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launch, spd_ensemble** out);
+/* Enqueue nlaunch graph launches (asynchronous). */
+int spd_ensemble_step(spd_ensemble* ens, int nlaunch);
+int spd_ensemble_synchronize(spd_ensemble* ens);
+/* Simulated time of instance i kept on the device (each step adds its dt). */
+int spd_ensemble_time(spd_ensemble* ens, int i, double* t_out);
+int spd_ensemble_set_time(spd_ensemble* ens, int i, double t);
+int spd_ensemble_destroy(spd_ensemble* ens);
+const char* spd_ensemble_last_error(const spd_ensemble* ens);
+/* Cells per thread block of the predictor's fused interior kernel (a power
+ * of two up to the shared-memory bound reported by the getter); a tuning
+ * knob of the ensemble autotuner, results are independent of it. */
+int spd_set_cells_per_block(spd_ctx* ctx, int cpb);
+int spd_get_cells_per_block(const spd_ctx* ctx, int* cpb, int* max_cpb);
+/* Every stride-th product of the kernels' contractions is computed on the
+ * integer pipes instead of the FP64 unit (same bits; 0 = none, 1 = all): a
+ * tuning knob that moves work off GB300's narrow FP64 pipe. */
+int spd_set_mul_stride(spd_ctx* ctx, int stride);
 
 #ifdef __cplusplus
 }

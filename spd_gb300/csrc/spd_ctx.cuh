@@ -31,6 +31,7 @@ struct spd_ctx {
   // state
   double *U_sp = nullptr, *U_cv = nullptr, *W_cv = nullptr, *U_new = nullptr;
   double* dt = nullptr;
+  double* t_dev = nullptr;  // simulated time kept on the device by the ensemble driver
   // predictor scratch
   double* U_ader = nullptr;
   double* trace[3] = {nullptr, nullptr, nullptr};
@@ -146,7 +147,8 @@ struct StepperBase {
   virtual int cmax(spd_ctx* C) = 0;      // dt from W_cv
   virtual int sp_to_cv(spd_ctx* C) = 0;  // U_cv = sp_to_cv(U_sp)
   virtual int configure(spd_ctx* C) = 0;
-  int cpb = 32;
+  int cpb = 32;       // cells per block of k_interior (a power of two <= max_cpb)
+  int max_cpb = 32;   // largest cpb whose shared-memory tile fits
   size_t smem = 0;
 };
 

@@ -1,0 +1,185 @@
+// Batched ensembles: many independent SD-ADER problems of different sizes
+// advanced together.  The per-instance step sequences (CFL dt reduction,
+// predictor, FV update, device-side time accumulation) are recorded once
+// into a CUDA graph whose branches run on several streams, so small
+// instances fill the GPU concurrently and a whole ensemble step costs one
+// graph launch instead of ~100 kernel launches and a host round trip per
+// instance.  Each instance keeps its own dt (its own device reduction).
+#include <memory>
+
+#include "spd_ctx.cuh"
+
+using namespace spd;
+using namespace spd_host;
+
+struct spd_ensemble {
+  std::vector<spd_ctx*> ctx;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> join;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int steps_per_launch = 1;
+  std::string err;
+};
+
+namespace {
+
+__global__ void k_time_add(double* t, const double* dt) { *t = *t + *dt; }
+
+int efail(spd_ensemble* E, int code, const std::string& msg) {
+  if (E) E->err = msg;
+  return code;
+}
+
+#define ECK(call)                                                                                   \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return efail(E, SPD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// one step of one instance on stream s, no host synchronisation
+int enqueue_step(spd_ctx* C, cudaStream_t s) {
+  cudaStream_t keep = C->stream;
+  C->stream = s;
+  int rc = C->stepper->cmax(C);
+  if (!rc) rc = C->stepper->update(C);
+  if (!rc) {
+    ProfScope ps_(C, "k_time_add");
+    k_time_add<<<1, 1, 0, s>>>(C->t_dev, C->dt);
+    if (cudaGetLastError() != cudaSuccess) rc = SPD_ERR_CUDA;
+  }
+  C->stream = keep;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launch, spd_ensemble** out) {
+  if (!ctxs || n <= 0 || nstreams <= 0 || steps_per_launch <= 0 || !out) return SPD_ERR_ARG;
+  std::unique_ptr<spd_ensemble> holder(new spd_ensemble());
+  spd_ensemble* E = holder.get();
+  E->steps_per_launch = steps_per_launch;
+  for (int i = 0; i < n; ++i) {
+    if (!ctxs[i]) return efail(E, SPD_ERR_ARG, "null context");
+    E->ctx.push_back(ctxs[i]);
+    spd_ctx* C = ctxs[i];
+    if (!C->t_dev) {
+      void* p = nullptr;
+      ECK(cudaMalloc(&p, sizeof(double)));
+      C->allocs.push_back(p);
+      C->t_dev = static_cast<double*>(p);
+    }
+    ECK(cudaStreamSynchronize(C->stream));
+    ECK(cudaMemset(C->t_dev, 0, sizeof(double)));
+  }
+  ECK(cudaStreamCreateWithFlags(&E->main, cudaStreamNonBlocking));
+  ECK(cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming));
+  E->streams.resize(nstreams);
+  E->join.resize(nstreams);
+  for (int s = 0; s < nstreams; ++s) {
+    ECK(cudaStreamCreateWithFlags(&E->streams[s], cudaStreamNonBlocking));
+    ECK(cudaEventCreateWithFlags(&E->join[s], cudaEventDisableTiming));
+  }
+  // longest-processing-time assignment of instances to streams (work ~ subcells)
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return E->ctx[a]->geo.Nq > E->ctx[b]->geo.Nq; });
+  std::vector<long long> load(nstreams, 0);
+  std::vector<int> lane(n, 0);
+  for (int i : order) {
+    int best = 0;
+    for (int s = 1; s < nstreams; ++s)
+      if (load[s] < load[best]) best = s;
+    lane[i] = best;
+    load[best] += E->ctx[i]->geo.Nq;
+  }
+  ECK(cudaStreamBeginCapture(E->main, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(E->fork, E->main);
+  for (int s = 0; s < nstreams; ++s) cudaStreamWaitEvent(E->streams[s], E->fork, 0);
+  int rc = 0;
+  for (int step = 0; step < steps_per_launch && !rc; ++step)
+    for (int i : order)
+      if (!rc) rc = enqueue_step(E->ctx[i], E->streams[lane[i]]);
+  for (int s = 0; s < nstreams; ++s) {
+    cudaEventRecord(E->join[s], E->streams[s]);
+    cudaStreamWaitEvent(E->main, E->join[s], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(E->main, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return efail(E, rc, "capture of an instance step failed");
+  }
+  if (ec != cudaSuccess) return efail(E, SPD_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ec));
+  E->graph = g;
+  ECK(cudaGraphInstantiate(&E->exec, E->graph, 0));
+  *out = holder.release();
+  return SPD_OK;
+}
+
+int spd_ensemble_step(spd_ensemble* E, int nlaunch) {
+  if (!E || nlaunch < 0) return SPD_ERR_ARG;
+  for (int i = 0; i < nlaunch; ++i) ECK(cudaGraphLaunch(E->exec, E->main));
+  return SPD_OK;
+}
+
+int spd_ensemble_synchronize(spd_ensemble* E) {
+  if (!E) return SPD_ERR_ARG;
+  ECK(cudaStreamSynchronize(E->main));
+  return SPD_OK;
+}
+
+int spd_ensemble_time(spd_ensemble* E, int i, double* t_out) {
+  if (!E || !t_out || i < 0 || i >= (int)E->ctx.size()) return SPD_ERR_ARG;
+  ECK(cudaStreamSynchronize(E->main));
+  ECK(cudaMemcpy(t_out, E->ctx[i]->t_dev, sizeof(double), cudaMemcpyDeviceToHost));
+  return SPD_OK;
+}
+
+int spd_ensemble_set_time(spd_ensemble* E, int i, double t) {
+  if (!E || i < 0 || i >= (int)E->ctx.size()) return SPD_ERR_ARG;
+  ECK(cudaStreamSynchronize(E->main));
+  ECK(cudaMemcpy(E->ctx[i]->t_dev, &t, sizeof(double), cudaMemcpyHostToDevice));
+  return SPD_OK;
+}
+
+int spd_ensemble_destroy(spd_ensemble* E) {
+  if (!E) return SPD_ERR_ARG;
+  if (E->main) cudaStreamSynchronize(E->main);
+  if (E->exec) cudaGraphExecDestroy(E->exec);
+  if (E->graph) cudaGraphDestroy(E->graph);
+  for (auto s : E->streams) cudaStreamDestroy(s);
+  for (auto e : E->join) cudaEventDestroy(e);
+  if (E->fork) cudaEventDestroy(E->fork);
+  if (E->main) cudaStreamDestroy(E->main);
+  delete E;
+  return SPD_OK;
+}
+
+const char* spd_ensemble_last_error(const spd_ensemble* E) { return E ? E->err.c_str() : "null ensemble"; }
+
+int spd_set_cells_per_block(spd_ctx* C, int cpb) {
+  if (!C || cpb < 1 || cpb > C->stepper->max_cpb || (cpb & (cpb - 1))) return SPD_ERR_ARG;
+  C->stepper->cpb = cpb;
+  return SPD_OK;
+}
+
+int spd_set_mul_stride(spd_ctx* C, int stride) {
+  if (!C || stride < 0) return SPD_ERR_ARG;
+  CK(cudaStreamSynchronize(C->stream));
+  C->geo.mul_stride = stride;
+  return SPD_OK;
+}
+
+int spd_get_cells_per_block(const spd_ctx* C, int* cpb, int* max_cpb) {
+  if (!C || !cpb || !max_cpb) return SPD_ERR_ARG;
+  *cpb = C->stepper->cpb;
+  *max_cpb = C->stepper->max_cpb;
+  return SPD_OK;
+}
+
+}  // extern "C"

@@ -52,9 +52,10 @@ struct Stepper : StepperBase {
   int configure(spd_ctx* C) override {
     // cells per block of the interior kernel: bounded by 200 KB of shared memory
     const size_t per_cell = (size_t)k::V * k::NS * C->T * sizeof(double);
-    cpb = 32;
-    while (cpb > 1 && per_cell * cpb > 200 * 1024) cpb /= 2;
-    smem = per_cell * cpb;
+    max_cpb = 64;
+    while (max_cpb > 1 && per_cell * max_cpb > 200 * 1024) max_cpb /= 2;
+    cpb = std::min(32, max_cpb);
+    smem = per_cell * max_cpb;
     CK(cudaFuncSetAttribute(k_interior<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
   }

@@ -1,0 +1,139 @@
+"""Batched ensembles of independent SD-ADER problems (no reference
+counterpart).
+
+``SDADER_Ensemble`` advances many ``SDADER_Simulator`` instances of
+different grid sizes together: the step of every instance -- its own CFL
+reduction, predictor, FV update -- is recorded once into a CUDA graph whose
+branches run on several streams (C ABI: ``spd_ensemble_*``), so one graph
+launch advances the whole ensemble.  ``autotune`` picks the number of
+streams and the cells per block of the predictor's fused kernel by timing
+real ensemble steps.  Every instance produces the same bits as stepping it
+alone.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+from . import _lib
+
+
+class SDADER_Ensemble:
+    def __init__(self, simulators, nstreams: int = 8, steps_per_launch: int = 1):
+        self.sims = list(simulators)
+        if not self.sims:
+            raise ValueError("empty ensemble")
+        self.lib = _lib.load()
+        self._declare()
+        self.nstreams = nstreams
+        self.steps_per_launch = steps_per_launch
+        self.tuning = None
+        self._ens = None
+        self._build()
+
+    def _declare(self):
+        lib = self.lib
+        vp = ctypes.c_void_p
+        lib.spd_ensemble_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(vp)]
+        lib.spd_ensemble_step.argtypes = [vp, ctypes.c_int]
+        lib.spd_ensemble_synchronize.argtypes = [vp]
+        lib.spd_ensemble_time.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.spd_ensemble_set_time.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+        lib.spd_ensemble_destroy.argtypes = [vp]
+        lib.spd_ensemble_last_error.argtypes = [vp]
+        lib.spd_ensemble_last_error.restype = ctypes.c_char_p
+        lib.spd_set_cells_per_block.argtypes = [vp, ctypes.c_int]
+        lib.spd_get_cells_per_block.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.lib.spd_ensemble_last_error(self._ens) if self._ens else b""
+            raise _lib.SpdError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
+
+    def _build(self):
+        self._close()
+        arr = (ctypes.c_void_p * len(self.sims))(*[s._ctx.h.value for s in self.sims])
+        h = ctypes.c_void_p()
+        rc = self.lib.spd_ensemble_create(arr, len(self.sims), self.nstreams, self.steps_per_launch, ctypes.byref(h))
+        if rc != 0:
+            raise _lib.SpdError(f"spd_ensemble_create failed with status {rc}")
+        self._ens = h
+
+    def _close(self):
+        if self._ens is not None and self._ens.value:
+            self.lib.spd_ensemble_destroy(self._ens)
+        self._ens = None
+
+    def _push_times(self):
+        """Start the device time accumulators from the instances' times, so
+        they add the dts exactly as the host loop does."""
+        for i, s in enumerate(self.sims):
+            self._check(self.lib.spd_ensemble_set_time(self._ens, i, float(s.time)), "set_time")
+
+    def _sync_times(self, steps):
+        self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
+        for i, s in enumerate(self.sims):
+            t = ctypes.c_double()
+            self._check(self.lib.spd_ensemble_time(self._ens, i, ctypes.byref(t)), "time")
+            s.time = t.value
+            s.n_step += steps
+
+    def cells_per_block(self):
+        out = []
+        for s in self.sims:
+            c, m = ctypes.c_int(), ctypes.c_int()
+            self.lib.spd_get_cells_per_block(s._ctx.h, ctypes.byref(c), ctypes.byref(m))
+            out.append((c.value, m.value))
+        return out
+
+    def set_cells_per_block(self, cpb: int):
+        for s in self.sims:
+            c, m = ctypes.c_int(), ctypes.c_int()
+            self.lib.spd_get_cells_per_block(s._ctx.h, ctypes.byref(c), ctypes.byref(m))
+            self.lib.spd_set_cells_per_block(s._ctx.h, min(cpb, m.value))
+
+    def perform_iterations(self, n_step: int) -> None:
+        """Advance every instance n_step steps (each with its own dt)."""
+        if n_step % self.steps_per_launch:
+            raise ValueError("n_step must be a multiple of steps_per_launch")
+        launches = n_step // self.steps_per_launch
+        self._push_times()
+        self._check(self.lib.spd_ensemble_step(self._ens, launches), "step")
+        self._sync_times(n_step)
+
+    def autotune(self, streams=(1, 2, 4, 8, 16, 32), cpbs=(16, 32, 64), probe_launches: int = 2):
+        """Time real ensemble steps for every (streams, cells per block)
+        candidate and keep the fastest.  The probe steps advance the
+        instances and count as steps."""
+        results = {}
+        for cpb in cpbs:
+            self.set_cells_per_block(cpb)
+            for ns in streams:
+                self.nstreams = ns
+                self._build()
+                self._push_times()
+                self._check(self.lib.spd_ensemble_step(self._ens, 1), "warm-up")
+                self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
+                t0 = time.perf_counter()
+                self._check(self.lib.spd_ensemble_step(self._ens, probe_launches), "probe")
+                self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
+                results[(ns, cpb)] = (time.perf_counter() - t0) / probe_launches
+                self._sync_times((1 + probe_launches) * self.steps_per_launch)
+        best = min(results, key=results.get)
+        self.nstreams, cpb = best
+        self.set_cells_per_block(cpb)
+        self._build()
+        self.tuning = {"streams": best[0], "cells_per_block": best[1],
+                       "seconds_per_step": results[best] / self.steps_per_launch,
+                       "candidates": {f"{k[0]}x{k[1]}": v for k, v in sorted(results.items())}}
+        return self.tuning
+
+    def close(self):
+        self._close()
+
+    def __del__(self):
+        try:
+            self._close()
+        except Exception:
+            pass
