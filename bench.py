@@ -35,6 +35,8 @@ WORKLOADS = {
                    "MUSCL-Hancock fallback, HLLC, transmissive boundaries",
     "vortex32": "isentropic vortex, 32x32 cells, p=3, FV update with limiting, LLF, periodic",
     "sedov128": "3D Sedov blast, 128^3 cells, p=2, FV update with limiting, HLLC, reflective",
+    "kh_ensemble": "batched: 64 periodic Kelvin-Helmholtz shear layers, p=3, sides drawn from "
+                   "{64,128,192,256,384,512} (seed 2026), HLLC + limiting, per-instance dt",
 }
 
 
@@ -252,8 +254,6 @@ def ours(args):
     dof, cells = dof_of(kw)
     s = SDADER_Simulator(verbose=False, **kw)
     ctx = s._ctx
-    if args.mul_stride is not None:
-        ctx.set_mul_stride(args.mul_stride)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     # warm-up
@@ -358,6 +358,56 @@ def ours(args):
         dist.destroy_process_group()
 
 
+def ensemble_arm(args):
+    """Batched ensemble vs the plain per-instance loop on the same instances."""
+    import numpy as np
+    import torch
+    from spd_gb300 import SDADER_Ensemble, SDADER_Simulator
+    from spd_gb300.initial_conditions import kelvin_helmholtz
+    rng = np.random.default_rng(2026)
+    sides = [int(x) for x in rng.choice([64, 128, 192, 256, 384, 512], size=args.instances)]
+
+    def make(i, n):
+        return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=1000 + i), update="FV", FB=True,
+                                riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                BC=(("periodic", "periodic"),) * 2, verbose=False)
+
+    sims = [make(i, n) for i, n in enumerate(sides)]
+    dof = sum(n * n * 16 for n in sides)
+    # plain per-instance loop (compute_dt + perform_update per instance and step)
+    for s in sims:
+        for _ in range(args.warmup):
+            s.compute_dt()
+            s.perform_update()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in sims:
+        for _ in range(args.steps):
+            s.compute_dt()
+            s.perform_update()
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    ens = SDADER_Ensemble(sims)
+    tuning = ens.autotune(streams=(1, 4, 16), cpbs=(32, 64), probe_launches=1)
+    ens.perform_iterations(args.warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.perform_iterations(args.steps)
+    batched_s = time.perf_counter() - t0
+    plain = dof * args.steps / plain_s
+    batched = dof * args.steps / batched_s
+    line = {"metric": METRIC + "; batched/plain speedup", "value": batched, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["kh_ensemble"], "instances": len(sides), "sides": sides,
+                       "dof_per_ensemble_step": dof},
+            "plain_loop_value": plain, "batched_over_plain": batched / plain, "autotune": tuning}
+    print(json.dumps(line), flush=True)
+    ens.close()
+    for s in sims:
+        s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,13 +416,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mul-stride", type=int, default=None,
-                    help="every k-th contraction product on the integer pipes (0 none, 1 all)")
+    ap.add_argument("--instances", type=int, default=64, help="ensemble size (kh_ensemble)")
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per direction (a smaller case of the workload, for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "kh_ensemble":
+        from spd_gb300.build import build
+        build()
+        ensemble_arm(args)
     else:
         from spd_gb300.build import build
         if int(os.environ.get("LOCAL_RANK", "0")) == 0:

@@ -154,12 +154,6 @@ int spd_profile_report(spd_ctx* ctx, char* buf, size_t len);
 /* Kernels launched by the context since it was created. */
 int spd_launch_count(const spd_ctx* ctx, long long* count);
 int spd_destroy(spd_ctx* ctx);
-/* Diagnostic: multiplies n generated operand pairs (all exponent ranges,
- * ties, sticky patterns, zeros, subnormals, infinities, NaNs) with the
- * kernels' integer-pipe binary64 multiply and with the FP64 unit, and
- * returns the number of results whose bits differ (expected 0).  No
- * reference counterpart. */
-int spd_selftest_fp64(long long n, unsigned long long seed, unsigned long long* mismatches_out);
 /* CFL time step dt = cfl_coeff * (h / max(ndim*c_s + sum |v|)) from
  * primitive subcell averages already on the device, without allocating
  * device memory.  No counterpart in the reference: it serves callers that
@@ -200,10 +194,6 @@ const char* spd_ensemble_last_error(const spd_ensemble* ens);
  * knob of the ensemble autotuner, results are independent of it. */
 int spd_set_cells_per_block(spd_ctx* ctx, int cpb);
 int spd_get_cells_per_block(const spd_ctx* ctx, int* cpb, int* max_cpb);
-/* Every stride-th product of the kernels' contractions is computed on the
- * integer pipes instead of the FP64 unit (same bits; 0 = none, 1 = all): a
- * tuning knob that moves work off GB300's narrow FP64 pipe. */
-int spd_set_mul_stride(spd_ctx* ctx, int stride);
 
 #ifdef __cplusplus
 }

@@ -31,9 +31,9 @@ EXPORTS = (
     "spd_get_dt", "spd_perform_update", "spd_step", "spd_end_sim",
     "spd_synchronize", "spd_destroy", "spd_last_error", "spd_version",
     "spd_set_stream", "spd_profile", "spd_profile_report", "spd_launch_count",
-    "spd_cfl_dt_noalloc", "spd_selftest_fp64", "spd_ensemble_create", "spd_ensemble_step",
+    "spd_cfl_dt_noalloc", "spd_ensemble_create", "spd_ensemble_step",
     "spd_ensemble_synchronize", "spd_ensemble_time", "spd_ensemble_set_time", "spd_ensemble_destroy", "spd_ensemble_last_error",
-    "spd_set_cells_per_block", "spd_get_cells_per_block", "spd_set_mul_stride",
+    "spd_set_cells_per_block", "spd_get_cells_per_block",
 )
 
 
@@ -114,7 +114,6 @@ def load():
     lib.spd_profile.argtypes = [vp, ctypes.c_int]
     lib.spd_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.spd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
-    lib.spd_set_mul_stride.argtypes = [vp, ctypes.c_int]
     lib.spd_last_error.restype = ctypes.c_char_p
     lib.spd_version.restype = ctypes.c_char_p
     for name in EXPORTS:
@@ -209,9 +208,6 @@ class Context:
             name, cnt, ms = line.split()
             out[name] = (int(cnt), float(ms))
         return out
-
-    def set_mul_stride(self, stride: int):
-        self.check(self.lib.spd_set_mul_stride(self.h, int(stride)), "set_mul_stride")
 
     def launch_count(self) -> int:
         n = ctypes.c_longlong()

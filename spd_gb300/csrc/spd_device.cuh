@@ -8,18 +8,8 @@
 #include <cstdint>
 #include <cmath>
 
-#include "spd_emul.cuh"
-
 namespace spd {
 
-// Product of term s of a contraction: the integer-pipe multiply (same bits
-// as the FP64 unit, see spd_emul.cuh) for every ``stride``-th term
-// (stride 0: none, 1: all), the FP64 unit otherwise -- a knob that splits
-// the multiplications between the FP64 pipe and the integer pipes.
-__device__ __forceinline__ double mulx(double a, double b, int s, int stride) {
-  if (stride > 0 && (s % stride) == stride - 1) return emul_mul(a, b);
-  return a * b;
-}
 
 constexpr int MAXN = 5;   // p <= 4
 constexpr int MAXNF = 6;
@@ -198,27 +188,27 @@ __device__ __forceinline__ void riemann(int solver, const double* ML, const doub
 // accumulated separately, then added); otherwise a left-to-right sum
 // (src/transforms.py:3-25).
 template <int L>
-__device__ __forceinline__ double dot_seq(const double* A, const double* x, int ms = 0) {
-  double acc = mulx(A[0], x[0], 0, ms);
+__device__ __forceinline__ double dot_seq(const double* A, const double* x) {
+  double acc = A[0] * x[0];
 #pragma unroll
-  for (int s = 1; s < L; ++s) acc = acc + mulx(A[s], x[s], s, ms);
+  for (int s = 1; s < L; ++s) acc = acc + A[s] * x[s];
   return acc;
 }
 template <int L>
-__device__ __forceinline__ double dot_lanes2(const double* A, const double* x, int ms = 0) {
-  double e = mulx(A[0], x[0], 0, ms);
+__device__ __forceinline__ double dot_lanes2(const double* A, const double* x) {
+  double e = A[0] * x[0];
   if (L == 1) return e;
-  double o = mulx(A[1], x[1], 1, ms);
+  double o = A[1] * x[1];
 #pragma unroll
   for (int s = 2; s < L; ++s) {
-    if (s % 2 == 0) e = e + mulx(A[s], x[s], s, ms);
-    else o = o + mulx(A[s], x[s], s, ms);
+    if (s % 2 == 0) e = e + A[s] * x[s];
+    else o = o + A[s] * x[s];
   }
   return e + o;
 }
 template <int L>
-__device__ __forceinline__ double dot_dir(const double* A, const double* x, int idim, int ms = 0) {
-  return idim == 0 ? dot_lanes2<L>(A, x, ms) : dot_seq<L>(A, x, ms);
+__device__ __forceinline__ double dot_dir(const double* A, const double* x, int idim) {
+  return idim == 0 ? dot_lanes2<L>(A, x) : dot_seq<L>(A, x);
 }
 
 // Limiters (src/muscl.py:12-59); NaN semantics follow the np.where forms.

@@ -168,13 +168,6 @@ int spd_set_cells_per_block(spd_ctx* C, int cpb) {
   return SPD_OK;
 }
 
-int spd_set_mul_stride(spd_ctx* C, int stride) {
-  if (!C || stride < 0) return SPD_ERR_ARG;
-  CK(cudaStreamSynchronize(C->stream));
-  C->geo.mul_stride = stride;
-  return SPD_OK;
-}
-
 int spd_get_cells_per_block(const spd_ctx* C, int* cpb, int* max_cpb) {
   if (!C || !cpb || !max_cpb) return SPD_ERR_ARG;
   *cpb = C->stepper->cpb;

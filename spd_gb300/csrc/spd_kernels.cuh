@@ -35,7 +35,6 @@ struct Geo {
   double h[3];
   double inv_h[3];  // 1/h, used only when h is a power of two (then x/h == x*(1/h) exactly)
   int h_pow2[3];
-  int mul_stride;   // every mul_stride-th contraction term on the integer pipes (0: none)
   double gamma, min_c2;
   int bc[3][2];
 };
@@ -92,8 +91,8 @@ __device__ __forceinline__ void write_traces(const Ops& op, const Geo& g, const 
 #pragma unroll
         for (int s = 0; s < k::n; ++s)
           x[s] = U[(((long long)v * Tu + tu) * k::NS + sp_index<D, P>(d, j, s)) * g.Nc + c];
-        const double l = dot_dir<k::n>(op.sp_to_fp, x, d, g.mul_stride);
-        const double r = dot_dir<k::n>(op.sp_to_fp + (k::nf - 1) * k::n, x, d, g.mul_stride);
+        const double l = dot_dir<k::n>(op.sp_to_fp, x, d);
+        const double r = dot_dir<k::n>(op.sp_to_fp + (k::nf - 1) * k::n, x, d);
         trace[d][(((long long)(0 * k::V + v) * g.T + t_out) * k::NJ + j) * g.Nc + c] = l;
         trace[d][(((long long)(1 * k::V + v) * g.T + t_out) * k::NJ + j) * g.Nc + c] = r;
       }
@@ -241,7 +240,7 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
         for (int f = 1; f < k::nf - 1; ++f) {
           double M[k::V], W[k::V], F[k::V];
 #pragma unroll
-          for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d, g.mul_stride);
+          for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
           prim<D>(M, W, g.gamma, 0);
           flux<D>(W, F, g.gamma, d);
 #pragma unroll
@@ -265,7 +264,7 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
           for (int v = 0; v < k::V; ++v) {
 #pragma unroll
             for (int so = 0; so < k::n; ++so) {
-              const double dsum = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d, g.mul_stride);
+              const double dsum = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d);
               const double val = pow2 ? dsum * ihd : dsum / hd;
               const int s = sp_index<D, P>(d, j, so);
               double* slot = &dudt_s[(((long long)v * k::NS + s) * Teff + tl) * CPB + cl];
@@ -351,7 +350,7 @@ __global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict
 #pragma unroll
         for (int a = 0; a < k::n; ++a) x[a] = G[a + k::n * b];
 #pragma unroll
-        for (int ao = 0; ao < k::n; ++ao) G1[ao + k::n * b] = dot_dir<k::n>(op.sp_to_cv + ao * k::n, x, o0, g.mul_stride);
+        for (int ao = 0; ao < k::n; ++ao) G1[ao + k::n * b] = dot_dir<k::n>(op.sp_to_cv + ao * k::n, x, o0);
       }
       if (D == 3) {
 #pragma unroll
@@ -360,7 +359,7 @@ __global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict
 #pragma unroll
           for (int b = 0; b < k::n; ++b) x[b] = G1[a + k::n * b];
 #pragma unroll
-          for (int bo = 0; bo < k::n; ++bo) G[a + k::n * bo] = dot_dir<k::n>(op.sp_to_cv + bo * k::n, x, o1, g.mul_stride);
+          for (int bo = 0; bo < k::n; ++bo) G[a + k::n * bo] = dot_dir<k::n>(op.sp_to_cv + bo * k::n, x, o1);
         }
       } else {
 #pragma unroll
@@ -390,21 +389,21 @@ __global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict
 //               input, src/sdader_simulator.py:302-307).
 // ---------------------------------------------------------------------------
 template <int D, int P>
-__device__ __forceinline__ double full_dot(const double* __restrict__ Krow, const double* x, bool rows, int ms) {
+__device__ __forceinline__ double full_dot(const double* __restrict__ Krow, const double* x, bool rows) {
   using k = K<D, P>;
-  if (D == 1) return dot_lanes2<k::n>(Krow, x, ms);
+  if (D == 1) return dot_lanes2<k::n>(Krow, x);
   if (rows || (D == 2 && k::n == 2)) {
     double acc = 0.0;
 #pragma unroll
     for (int r = 0; r < k::NS / k::n; ++r) {
-      double rs = mulx(Krow[r * k::n], x[r * k::n], 0, ms);
+      double rs = Krow[r * k::n] * x[r * k::n];
 #pragma unroll
-      for (int l = 1; l < k::n; ++l) rs = rs + mulx(Krow[r * k::n + l], x[r * k::n + l], l, ms);
+      for (int l = 1; l < k::n; ++l) rs = rs + Krow[r * k::n + l] * x[r * k::n + l];
       acc = (r == 0) ? rs : acc + rs;
     }
     return acc;
   }
-  return dot_seq<k::NS>(Krow, x, ms);
+  return dot_seq<k::NS>(Krow, x);
 }
 
 // U_cv (FV layout) = sp_to_cv(U_sp) for every cell and variable
@@ -425,7 +424,7 @@ __global__ void k_sp_to_cv(Geo g, const double* __restrict__ Kfull, const double
     const int kx = o % k::n, ky = (o / k::n) % k::n, kz = o / (k::n * k::n);
     const long long q = (cx * k::n + kx) + (long long)g.X[0] * ((D >= 2 ? cy * k::n + ky : 0) +
                                                                (long long)g.X[1] * (D >= 3 ? cz * k::n + kz : 0));
-    U_cv[(long long)v * g.Nq + q] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, false, g.mul_stride);
+    U_cv[(long long)v * g.Nq + q] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, false);
   }
 }
 
@@ -448,7 +447,7 @@ __global__ void k_cv_to_sp(Geo g, const double* __restrict__ Kfull, const double
                                                                (long long)g.X[1] * (D >= 3 ? cz * k::n + kz : 0));
     x[s] = U_cv[(long long)v * g.Nq + q];
   }
-  for (int o = 0; o < k::NS; ++o) U_sp[((long long)v * k::NS + o) * g.Nc + c] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, true, g.mul_stride);
+  for (int o = 0; o < k::NS; ++o) U_sp[((long long)v * k::NS + o) * g.Nc + c] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, true);
 }
 
 }  // namespace spd

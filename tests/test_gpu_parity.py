@@ -168,17 +168,3 @@ def test_quadrant_512_one_step_full_size_bitwise():
                                    BC=(("gradfree", "gradfree"),) * 2)
     assert troubles > 0
     assert not bad, bad
-
-
-@pytest.mark.parametrize("stride", [1, 2, 3])
-def test_integer_pipe_products_keep_bits(stride):
-    """Moving contraction products to the integer pipes changes no bit."""
-    from spd_gb300 import SDADER_Simulator
-    from spd_gb300.initial_conditions import four_quadrant
-    s = SDADER_Simulator(p=3, N=(24, 24), init_fct=four_quadrant, update="FV", FB=True, riemann_solver_sd="hllc",
-                         riemann_solver_fv="hllc", BC=(("gradfree", "gradfree"),) * 2, verbose=False)
-    s._ctx.set_mul_stride(stride)
-    o = oracle_like(s)
-    step_both(s, o, 3)
-    assert not compare(s, o)
-    s.close()
