@@ -70,7 +70,8 @@ enum spd_field {
   SPD_BC_FP_Z = 10,
   SPD_BC_FV_X = 11,
   SPD_BC_FV_Y = 12,
-  SPD_BC_FV_Z = 13
+  SPD_BC_FV_Z = 13,
+  SPD_U_SP_ADJ = 14  /* adjoint of U_sp (U_sp layout), input and output of spd_vjp_step */
 };
 
 /* Constructor options of SDADER_Simulator (src/simulator.py:10-36,
@@ -194,6 +195,36 @@ const char* spd_ensemble_last_error(const spd_ensemble* ens);
  * knob of the ensemble autotuner, results are independent of it. */
 int spd_set_cells_per_block(spd_ctx* ctx, int cpb);
 int spd_get_cells_per_block(const spd_ctx* ctx, int* cpb, int* max_cpb);
+
+/* ---- adjoint (no reference counterpart) --------------------------------
+ * Vector-Jacobian product of one SD-ADER step U_sp -> U_sp'.  The step is
+ * differentiated with dt, the trouble masks, theta, the affected faces, the
+ * slope-limiter branches and the Riemann-solver branches frozen at their
+ * values in a recorded forward step.
+ * spd_adjoint_enable allocates ``depth`` record slots (the forward
+ * intermediates of one step each: U_sp, the Picard iterates, the FV substep
+ * states and affected faces) and the adjoint work arrays.
+ * spd_record_step advances U_sp by one step with the given dt (no CFL
+ * reduction) and records it into ``slot``; the step is bit-identical to
+ * spd_set_dt + spd_perform_update.
+ * spd_vjp_step replaces the SPD_U_SP_ADJ field a by J^T a, J the Jacobian of
+ * the step recorded in ``slot``.
+ * Decision tapes (for finite-difference checks of the adjoint):
+ * spd_tape_enable allocates tapes for ``nsteps`` steps; spd_tape_step
+ * advances U_sp by one step with the given dt and, with mode 1, records the
+ * step's decisions into tape ``step`` (the affected faces and the branch
+ * outcomes of every Riemann problem and limited slope) or, with mode 2,
+ * replays them instead of taking them: the frozen-decision step whose
+ * Jacobian spd_vjp_step applies.  Mode 1 is bit-identical to
+ * spd_set_dt + spd_perform_update.
+ * Uploads and downloads of U_sp, U_cv, W_cv and SPD_U_SP_ADJ accept host or
+ * device pointers. */
+int spd_adjoint_enable(spd_ctx* ctx, int depth);
+int spd_adjoint_depth(const spd_ctx* ctx, int* depth);
+int spd_record_step(spd_ctx* ctx, int slot, double dt);
+int spd_vjp_step(spd_ctx* ctx, int slot);
+int spd_tape_enable(spd_ctx* ctx, int nsteps);
+int spd_tape_step(spd_ctx* ctx, int step, double dt, int mode);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ FIELD = {
     "U_sp": 0, "U_cv": 1, "W_cv": 2, "troubles": 3, "theta": 4,
     "affected_faces_x": 5, "affected_faces_y": 6, "affected_faces_z": 7,
     "BC_fp_x": 8, "BC_fp_y": 9, "BC_fp_z": 10,
-    "BC_fv_x": 11, "BC_fv_y": 12, "BC_fv_z": 13,
+    "BC_fv_x": 11, "BC_fv_y": 12, "BC_fv_z": 13, "U_sp_adj": 14,
 }
 
 # every entry point declared in include/spd_gb300.h
@@ -34,6 +34,8 @@ EXPORTS = (
     "spd_cfl_dt_noalloc", "spd_ensemble_create", "spd_ensemble_step",
     "spd_ensemble_synchronize", "spd_ensemble_time", "spd_ensemble_set_time", "spd_ensemble_destroy", "spd_ensemble_last_error",
     "spd_set_cells_per_block", "spd_get_cells_per_block",
+    "spd_adjoint_enable", "spd_adjoint_depth", "spd_record_step", "spd_vjp_step",
+    "spd_tape_enable", "spd_tape_step",
 )
 
 
@@ -114,6 +116,12 @@ def load():
     lib.spd_profile.argtypes = [vp, ctypes.c_int]
     lib.spd_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.spd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    lib.spd_adjoint_enable.argtypes = [vp, ctypes.c_int]
+    lib.spd_adjoint_depth.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    lib.spd_record_step.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    lib.spd_vjp_step.argtypes = [vp, ctypes.c_int]
+    lib.spd_tape_enable.argtypes = [vp, ctypes.c_int]
+    lib.spd_tape_step.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.spd_last_error.restype = ctypes.c_char_p
     lib.spd_version.restype = ctypes.c_char_p
     for name in EXPORTS:
@@ -161,6 +169,37 @@ class Context:
         out = np.empty(shape, dtype=np.float64)
         self.check(self.lib.spd_download(self.h, FIELD[field], as_ptr(out), out.size), f"download {field}")
         return out
+
+    def upload_ptr(self, field: str, ptr: int, count: int):
+        """Upload from a host or device address (count doubles, reference layout)."""
+        self.check(self.lib.spd_upload(self.h, FIELD[field], ctypes.cast(ctypes.c_void_p(ptr), _dp), int(count)),
+                   f"upload {field}")
+
+    def download_ptr(self, field: str, ptr: int, count: int):
+        """Download into a host or device address (count doubles, reference layout)."""
+        self.check(self.lib.spd_download(self.h, FIELD[field], ctypes.cast(ctypes.c_void_p(ptr), _dp), int(count)),
+                   f"download {field}")
+
+    def adjoint_enable(self, depth: int):
+        self.check(self.lib.spd_adjoint_enable(self.h, int(depth)), "adjoint_enable")
+
+    def adjoint_depth(self) -> int:
+        n = ctypes.c_int()
+        self.check(self.lib.spd_adjoint_depth(self.h, ctypes.byref(n)), "adjoint_depth")
+        return n.value
+
+    def record_step(self, slot: int, dt: float):
+        self.check(self.lib.spd_record_step(self.h, int(slot), float(dt)), "record_step")
+
+    def vjp_step(self, slot: int):
+        self.check(self.lib.spd_vjp_step(self.h, int(slot)), "vjp_step")
+
+    def tape_enable(self, nsteps: int):
+        self.check(self.lib.spd_tape_enable(self.h, int(nsteps)), "tape_enable")
+
+    def tape_step(self, step: int, dt: float, mode: int):
+        """mode 1: step and record its decisions; mode 2: step replaying them."""
+        self.check(self.lib.spd_tape_step(self.h, int(step), float(dt), int(mode)), "tape_step")
 
     def compute_dt(self) -> float:
         dt = ctypes.c_double()

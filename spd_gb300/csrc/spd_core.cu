@@ -284,6 +284,8 @@ int spd_destroy(spd_ctx* C) {
   if (!C) return SPD_ERR_ARG;
   if (C->stream) cudaStreamSynchronize(C->stream);
   for (void* p : C->allocs) cudaFree(p);
+  for (void* p : C->adj_allocs) cudaFree(p);
+  for (void* p : C->tape_allocs) cudaFree(p);
   for (auto& r : C->rec) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -359,6 +361,7 @@ static size_t field_count(spd_ctx* C, int field) {
     case SPD_U_SP:
     case SPD_U_CV:
     case SPD_W_CV: return (size_t)V * C->NS * g.Nc;
+    case SPD_U_SP_ADJ: return C->Usp_a ? (size_t)V * C->NS * g.Nc : 0;
     case SPD_TROUBLES: return (size_t)g.Nq;
     case SPD_THETA: return (size_t)g.Nqe;
     case SPD_AFFECTED_X:
@@ -411,12 +414,13 @@ int spd_upload(spd_ctx* C, int field, const double* host, size_t count) {
   const size_t need = field_count(C, field);
   if (need == 0 || count != need) return fail(C, SPD_ERR_ARG, "upload: wrong field or element count");
   const Geo& g = C->geo;
-  if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV) {
+  if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV || field == SPD_U_SP_ADJ) {
     if (int r = ensure_staging(C, need)) return r;
-    CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyHostToDevice, C->stream));
-    double* dst = (field == SPD_U_SP) ? C->U_sp : (field == SPD_U_CV ? C->U_cv : C->W_cv);
+    CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyDefault, C->stream));
+    double* dst = (field == SPD_U_SP) ? C->U_sp
+                  : (field == SPD_U_CV ? C->U_cv : (field == SPD_W_CV ? C->W_cv : C->Usp_a));
     k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, C->staging, dst, 1,
-                                                                       field == SPD_U_SP ? 0 : 1);
+                                                                       (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
     CKL();
     CK(cudaStreamSynchronize(C->stream));
     return SPD_OK;
@@ -453,13 +457,14 @@ int spd_download(spd_ctx* C, int field, double* host, size_t count) {
   const size_t need = field_count(C, field);
   if (need == 0 || count != need) return fail(C, SPD_ERR_ARG, "download: wrong field or element count");
   const Geo& g = C->geo;
-  if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV) {
+  if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV || field == SPD_U_SP_ADJ) {
     if (int r = ensure_staging(C, need)) return r;
-    const double* src = (field == SPD_U_SP) ? C->U_sp : (field == SPD_U_CV ? C->U_cv : C->W_cv);
-    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, src, C->staging, 0,
-                                                                       field == SPD_U_SP ? 0 : 1);
+    const double* src = (field == SPD_U_SP) ? C->U_sp
+                        : (field == SPD_U_CV ? C->U_cv : (field == SPD_W_CV ? C->W_cv : C->Usp_a));
+    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(
+        g, C->D, C->n, C->V, src, C->staging, 0, (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
     CKL();
-    CK(cudaMemcpyAsync(host, C->staging, need * sizeof(double), cudaMemcpyDeviceToHost, C->stream));
+    CK(cudaMemcpyAsync(host, C->staging, need * sizeof(double), cudaMemcpyDefault, C->stream));
     CK(cudaStreamSynchronize(C->stream));
     return SPD_OK;
   }

@@ -32,6 +32,39 @@ struct spd_ctx {
   double *U_sp = nullptr, *U_cv = nullptr, *W_cv = nullptr, *U_new = nullptr;
   double* dt = nullptr;
   double* t_dev = nullptr;  // simulated time kept on the device by the ensemble driver
+  // adjoint: record slots of forward intermediates and the adjoint work
+  // arrays (allocated by spd_adjoint_enable, freed on re-enable and destroy)
+  bool recording = false;
+  // decision tapes: per step, the affected faces and the branch outcomes of
+  // every Riemann problem and limited slope (spd_tape_enable / spd_tape_step)
+  int tape_mode = 0;  // 0 off, 1 record, 2 replay
+  int tape_step = 0, tape_steps = 0;
+  std::vector<void*> tape_allocs;
+  unsigned* tape_rs[3] = {nullptr, nullptr, nullptr};
+  unsigned* tape_fb[3] = {nullptr, nullptr, nullptr};
+  unsigned char* tape_lim = nullptr;
+  double* tape_aff = nullptr;
+  int adj_depth = 0;
+  std::vector<void*> adj_allocs;
+  size_t rec_usp_n = 0, rec_ader_n = 0, rec_ucv_n = 0, rec_aff_n = 0;
+  double *rec_usp = nullptr, *rec_ader = nullptr, *rec_ucv = nullptr, *rec_aff = nullptr, *rec_dt = nullptr;
+  double* hist_usp = nullptr;   // U_sp at the start of the recorded step
+  double* hist_ader = nullptr;  // U_ader after each Picard iteration but the last (m slots)
+  double* hist_ucv = nullptr;   // U_cv at the start of each FV substep (T slots)
+  double* hist_aff = nullptr;   // affected faces of each substep (T slots, all directions)
+  double* hist_dt = nullptr;    // dt of the recorded step
+  double* Usp_a = nullptr;
+  double* Ua = nullptr;
+  double* dudt_a = nullptr;
+  double* Ea[3] = {nullptr, nullptr, nullptr};
+  double* Tra[3] = {nullptr, nullptr, nullptr};
+  double* Ffa[3] = {nullptr, nullptr, nullptr};
+  double* FHa[3] = {nullptr, nullptr, nullptr};
+  double* Fba[3] = {nullptr, nullptr, nullptr};
+  double* FA[3] = {nullptr, nullptr, nullptr};  // reconstructed-state adjoints per fallback face
+  double* LA = nullptr;                          // limiter adjoints per extended cell
+  double *Ucv_a = nullptr, *Unew_a = nullptr, *W_a = nullptr, *W_ext = nullptr;
+  double* bcbuf_a[3] = {nullptr, nullptr, nullptr};
   // predictor scratch
   double* U_ader = nullptr;
   double* trace[3] = {nullptr, nullptr, nullptr};
@@ -147,6 +180,7 @@ struct StepperBase {
   virtual int cmax(spd_ctx* C) = 0;      // dt from W_cv
   virtual int sp_to_cv(spd_ctx* C) = 0;  // U_cv = sp_to_cv(U_sp)
   virtual int configure(spd_ctx* C) = 0;
+  virtual int vjp(spd_ctx* C) = 0;       // Usp_a <- (d U_sp_new / d U_sp)^T Usp_a of the recorded step
   int cpb = 32;       // cells per block of k_interior (a power of two <= max_cpb)
   int max_cpb = 32;   // largest cpb whose shared-memory tile fits
   size_t smem = 0;

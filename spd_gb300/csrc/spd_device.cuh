@@ -20,9 +20,155 @@ enum Riemann : int { RS_LLF = 0, RS_HLLC = 1, RS_LHLLC = 2 };
 enum Limiter : int { LIM_MINMOD = 0, LIM_MONCEN = 1 };
 enum BcKind : int { BC_PERIODIC = 0, BC_REFLECTIVE = 1, BC_GRADFREE = 2, BC_IC = 3, BC_EQ = 4, BC_PRESSURE = 5 };
 
+// ---------------------------------------------------------------------------
+// Scalars: the physics below is written for a generic scalar S, instantiated
+// with double (the step itself, same arithmetic as written) and with the
+// forward-mode dual number Dual<N> (value plus N tangents), which the
+// adjoint kernels use for the Jacobian-transpose products of local maps.
+// ---------------------------------------------------------------------------
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+  __device__ __forceinline__ Dual() {}
+  __device__ __forceinline__ Dual(double x) : v(x) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = 0.0;
+  }
+};
+template <int N>
+__device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r; r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r; r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r; r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r; r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r; r.v = a.v / b.v;
+  const double ib = 1.0 / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, double b) { return a + Dual<N>(b); }
+template <int N> __device__ __forceinline__ Dual<N> operator+(double a, const Dual<N>& b) { return Dual<N>(a) + b; }
+template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, double b) { return a - Dual<N>(b); }
+template <int N> __device__ __forceinline__ Dual<N> operator-(double a, const Dual<N>& b) { return Dual<N>(a) - b; }
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, double b) {
+  Dual<N> r; r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
+  return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator*(double a, const Dual<N>& b) { return b * a; }
+template <int N> __device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, double b) { return a / Dual<N>(b); }
+template <int N> __device__ __forceinline__ Dual<N> operator/(double a, const Dual<N>& b) { return Dual<N>(a) / b; }
+template <int N> __device__ __forceinline__ bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
+template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
+template <int N> __device__ __forceinline__ bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
+template <int N> __device__ __forceinline__ bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
+template <int N> __device__ __forceinline__ bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
+template <int N> __device__ __forceinline__ bool operator<(const Dual<N>& a, double b) { return a.v < b; }
+template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, double b) { return a.v > b; }
+
+__device__ __forceinline__ double sval(double x) { return x; }
+template <int N> __device__ __forceinline__ double sval(const Dual<N>& x) { return x.v; }
+__device__ __forceinline__ double ad_sqrt(double x) { return sqrt(x); }
+template <int N>
+__device__ __forceinline__ Dual<N> ad_sqrt(const Dual<N>& x) {
+  Dual<N> r; r.v = sqrt(x.v);
+  const double k = 0.5 / r.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
+  return r;
+}
+__device__ __forceinline__ double ad_abs(double x) { return fabs(x); }
+template <int N>
+__device__ __forceinline__ Dual<N> ad_abs(const Dual<N>& x) {
+  if (x.v > 0) return x;
+  if (x.v < 0) return -x;
+  return Dual<N>(fabs(x.v));
+}
+
 // NumPy's maximum / minimum: NaN in either argument propagates.
-__device__ __forceinline__ double np_max(double a, double b) { return (a >= b || a != a) ? a : b; }
-__device__ __forceinline__ double np_min(double a, double b) { return (a <= b || a != a) ? a : b; }
+template <class S>
+__device__ __forceinline__ S np_max(const S& a, const S& b) { return (a >= b || a != a) ? a : b; }
+template <class S>
+__device__ __forceinline__ S np_min(const S& a, const S& b) { return (a <= b || a != a) ? a : b; }
+// Dual forms: same value; at a tie the derivative is the mean of the two
+// arguments' derivatives (the subgradient torch.maximum / torch.minimum
+// propagate).
+template <int N>
+__device__ __forceinline__ Dual<N> tie_mean(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = 0.5 * (a.d[i] + b.d[i]);
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> np_max(const Dual<N>& a, const Dual<N>& b) {
+  if (a.v == b.v) return tie_mean(a, b);
+  return (a.v >= b.v || a.v != a.v) ? a : b;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> np_min(const Dual<N>& a, const Dual<N>& b) {
+  if (a.v == b.v) return tie_mean(a, b);
+  return (a.v <= b.v || a.v != a.v) ? a : b;
+}
+
+// Branch control of the piecewise-smooth maps (Riemann solvers, slope
+// limiters).  BM = 0: live comparisons (the step); BM = 1: live, and each
+// comparison's outcome is appended to ``w`` (a decision tape word);
+// BM = 2: the outcomes are read back from ``w`` instead of compared, which
+// evaluates the same smooth branch at a perturbed state (the frozen-branch
+// map that the adjoint differentiates).
+template <int BM>
+struct Br {
+  unsigned w = 0;
+  int k = 0;
+};
+template <int BM>
+__device__ __forceinline__ bool pick(Br<BM>* br, bool live) {
+  if (BM == 0) return live;
+  if (BM == 1) {
+    if (live) br->w |= (1u << br->k);
+    ++br->k;
+    return live;
+  }
+  const bool b = (br->w >> br->k) & 1u;
+  ++br->k;
+  return b;
+}
+// |x| whose sign is a recorded decision under BM != 0
+template <int BM, class S>
+__device__ __forceinline__ S abs_br(const S& x, Br<BM>* br) {
+  if (BM == 0) return ad_abs(x);
+  return pick(br, sval(x) >= 0.0) ? x : -x;
+}
 
 // Velocity index k (0-based) of the rotated frame used for direction idim:
 // np.roll(vels, -idim) (src/sdader_simulator.py:219).
@@ -32,16 +178,16 @@ __device__ __forceinline__ int rvel(int idim, int k) { return 1 + (idim + k) % D
 // U -> W (src/hydro.py:48-86); the kinetic term sums in the order of the
 // velocity list, which is the rotated list inside the Riemann wrapper
 // (src/riemann_solver.py:10-29) and the plain list elsewhere.
-template <int D>
-__device__ __forceinline__ void prim(const double* U, double* W, double gamma, int idim_order) {
+template <int D, class S>
+__device__ __forceinline__ void prim(const S* U, S* W, double gamma, int idim_order) {
   constexpr int P_ = D + 1;
   W[0] = U[0];
-  double K = 0.0;
+  S K = 0.0;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const int v = rvel<D>(idim_order, k);
     W[v] = U[v] / U[0];
-    const double w2 = W[v] * W[v];
+    const S w2 = W[v] * W[v];
     K = (k == 0) ? w2 : K + w2;
   }
   K = K * (0.5 * U[0]);
@@ -49,16 +195,16 @@ __device__ __forceinline__ void prim(const double* U, double* W, double gamma, i
 }
 
 // W -> U (src/hydro.py:88-125).
-template <int D>
-__device__ __forceinline__ void cons(const double* W, double* U, double gamma, int idim_order) {
+template <int D, class S>
+__device__ __forceinline__ void cons(const S* W, S* U, double gamma, int idim_order) {
   constexpr int P_ = D + 1;
   U[0] = W[0];
-  double K = 0.0;
+  S K = 0.0;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const int v = rvel<D>(idim_order, k);
     U[v] = W[v] * W[0];
-    const double w2 = W[v] * W[v];
+    const S w2 = W[v] * W[v];
     K = (k == 0) ? w2 : K + w2;
   }
   K = K * (0.5 * W[0]);
@@ -66,85 +212,94 @@ __device__ __forceinline__ void cons(const double* W, double* U, double gamma, i
 }
 
 // Euler flux in the rotated frame of direction idim (src/hydro.py:127-170).
-template <int D>
-__device__ __forceinline__ void flux(const double* W, double* F, double gamma, int idim) {
+template <int D, class S>
+__device__ __forceinline__ void flux(const S* W, S* F, double gamma, int idim) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
-  double K = 0.0, m = 0.0;
+  S K = 0.0, m = 0.0;
 #pragma unroll
   for (int k = D - 1; k >= 0; --k) {
     const int v = rvel<D>(idim, k);
     m = W[0] * W[v];
-    const double mv = m * W[v];
+    const S mv = m * W[v];
     K = (k == D - 1) ? mv : K + mv;
     F[v] = m * W[v1];
   }
-  const double E = W[P_] / (gamma - 1.0) + 0.5 * K;
+  const S E = W[P_] / (gamma - 1.0) + 0.5 * K;
   F[0] = m;
   F[v1] = m * W[v1] + W[P_];
   F[P_] = W[v1] * (E + W[P_]);
 }
 
 // Sound speed with floor (src/hydro.py:3-46).
-__device__ __forceinline__ double sound_speed(double P, double rho, double gamma, double min_c2) {
-  double c2 = gamma * P / rho;
-  c2 = (c2 > min_c2) ? c2 : min_c2;
-  return sqrt(c2);
+template <class S, int BM = 0>
+__device__ __forceinline__ S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
+                                         Br<BM>* br = nullptr) {
+  S c2 = gamma * P / rho;
+  c2 = pick(br, c2 > min_c2) ? c2 : S(min_c2);
+  return ad_sqrt(c2);
 }
 
 // LLF (src/riemann_solver.py:31-65).
-template <int D>
-__device__ __forceinline__ void llf(const double* WL, const double* WR, const double* UL, const double* UR,
-                                    double* F, double gamma, double min_c2, int idim) {
+template <int D, class S, int BM = 0>
+__device__ __forceinline__ void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
+                                    double min_c2, int idim, Br<BM>* br = nullptr) {
   constexpr int V = D + 2, P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
-  double FL[V], FR[V];
+  S FL[V], FR[V];
   flux<D>(WL, FL, gamma, idim);
   flux<D>(WR, FR, gamma, idim);
-  const double cL = sound_speed(WL[P_], WL[0], gamma, min_c2) + fabs(WL[v1]);
-  const double cR = sound_speed(WR[P_], WR[0], gamma, min_c2) + fabs(WR[v1]);
-  const double cmax = (cL > cR) ? cL : cR;
-  const double hc = 0.5 * cmax;
+  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br) + abs_br(WL[v1], br);
+  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br) + abs_br(WR[v1], br);
+  const S cmax = pick(br, cL > cR) ? cL : cR;
+  const S hc = 0.5 * cmax;
 #pragma unroll
   for (int v = 0; v < V; ++v) F[v] = 0.5 * (FR[v] + FL[v]) - hc * (UR[v] - UL[v]);
 }
 
 // HLLC (src/riemann_solver.py:67-145) and its low-Mach variant (:147-212).
 // Only the branch the reference's np.where chain selects is evaluated.
-template <int D>
-__device__ __forceinline__ void hllc(const double* WL, const double* WR, const double* UL, const double* UR,
-                                     double* F, double gamma, double min_c2, int idim, bool low_mach) {
+template <int D, class S, int BM = 0>
+__device__ __forceinline__ void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
+                                     double min_c2, int idim, bool low_mach, Br<BM>* br = nullptr) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
-  const double cL = sound_speed(WL[P_], WL[0], gamma, min_c2) + fabs(WL[v1]);
-  const double cR = sound_speed(WR[P_], WR[0], gamma, min_c2) + fabs(WR[v1]);
-  const double cmax = (cL > cR) ? cL : cR;
-  const double vL = WL[v1], vR = WR[v1];
-  const double sL = ((vL < vR) ? vL : vR) - cmax;
-  const double sR = ((vL > vR) ? vL : vR) + cmax;
-  const double rcL = WL[0] * (vL - sL);
-  const double rcR = WR[0] * (sR - vR);
-  const double den = rcR + rcL;
-  const double vstar = (rcR * vR + rcL * vL + (WL[P_] - WR[P_])) / den;
-  double Pstar;
+  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br) + abs_br(WL[v1], br);
+  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br) + abs_br(WR[v1], br);
+  const S cmax = pick(br, cL > cR) ? cL : cR;
+  const S vL = WL[v1], vR = WR[v1];
+  const S sL = (pick(br, vL < vR) ? vL : vR) - cmax;
+  const S sR = (pick(br, vL > vR) ? vL : vR) + cmax;
+  const S rcL = WL[0] * (vL - sL);
+  const S rcR = WR[0] * (sR - vR);
+  const S den = rcR + rcL;
+  const S vstar = (rcR * vR + rcL * vL + (WL[P_] - WR[P_])) / den;
+  S Pstar;
   if (low_mach) {
-    const double mx = np_max(fabs(vL), fabs(vR)) / cmax;
-    const double Mach = np_min(1.0, mx);
-    const double phi = Mach * (2.0 - Mach);
+    S mx, Mach;
+    if (BM == 0) {
+      mx = np_max(ad_abs(vL), ad_abs(vR)) / cmax;
+      Mach = np_min(S(1.0), mx);
+    } else {
+      const S aL = abs_br(vL, br), aR = abs_br(vR, br);
+      mx = (pick(br, aL >= aR || aL != aL) ? aL : aR) / cmax;
+      Mach = pick(br, S(1.0) <= mx) ? S(1.0) : mx;
+    }
+    const S phi = Mach * (2.0 - Mach);
     Pstar = (rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR)) / den;
   } else {
     Pstar = (rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR)) / den;
   }
-  double r, vg, Pg, e;
-  if (sL > 0) {
+  S r, vg, Pg, e;
+  if (pick(br, sL > 0.0)) {
     r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
-  } else if (vstar > 0) {
-    const double d = sL - vstar;
+  } else if (pick(br, vstar > 0.0)) {
+    const S d = sL - vstar;
     r = WL[0] * (sL - vL) / d;
     e = ((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar) / d;
     vg = vstar; Pg = Pstar;
-  } else if (sR > 0) {
-    const double d = sR - vstar;
+  } else if (pick(br, sR > 0.0)) {
+    const S d = sR - vstar;
     r = WR[0] * (sR - vR) / d;
     e = ((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar) / d;
     vg = vstar; Pg = Pstar;
@@ -154,20 +309,23 @@ __device__ __forceinline__ void hllc(const double* WL, const double* WR, const d
   F[0] = r * vg;
   F[v1] = F[0] * vg + Pg;
   F[P_] = vg * (e + Pg);
+  if (D > 1) {
+    const bool left = pick(br, vstar > 0.0);
 #pragma unroll
-  for (int k = 1; k < D; ++k) {
-    const int v = rvel<D>(idim, k);
-    F[v] = F[0] * ((vstar > 0) ? WL[v] : WR[v]);
+    for (int k = 1; k < D; ++k) {
+      const int v = rvel<D>(idim, k);
+      F[v] = F[0] * (left ? WL[v] : WR[v]);
+    }
   }
 }
 
 // Riemann wrapper (src/riemann_solver.py:10-29): inputs conservative
 // (prims=false) or primitive (prims=true); rotated velocity order.
-template <int D>
-__device__ __forceinline__ void riemann(int solver, const double* ML, const double* MR, double* F, double gamma,
-                                        double min_c2, int idim, bool prims) {
+template <int D, class S, int BM = 0>
+__device__ __forceinline__ void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, double min_c2,
+                                        int idim, bool prims, Br<BM>* br = nullptr) {
   constexpr int V = D + 2;
-  double WL[V], WR[V], UL[V], UR[V];
+  S WL[V], WR[V], UL[V], UR[V];
   if (prims) {
 #pragma unroll
     for (int v = 0; v < V; ++v) { WL[v] = ML[v]; WR[v] = MR[v]; }
@@ -179,8 +337,8 @@ __device__ __forceinline__ void riemann(int solver, const double* ML, const doub
     prim<D>(UL, WL, gamma, idim);
     prim<D>(UR, WR, gamma, idim);
   }
-  if (solver == RS_LLF) llf<D>(WL, WR, UL, UR, F, gamma, min_c2, idim);
-  else hllc<D>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC);
+  if (solver == RS_LLF) llf<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, br);
+  else hllc<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC, br);
 }
 
 // One output of a 1D operator contraction: sum_s A[s] * x[s].  ``lanes2``
@@ -225,6 +383,50 @@ __device__ __forceinline__ double moncen(double dUL, double dUR, double dxL, dou
   double slope = np_min(fabs(2.0 * dUL * dxL / dxM), fabs(2.0 * dUR * dxR / dxM));
   slope = np_sign(dUC) * np_min(slope, fabs(dUC));
   return (dUL * dUR >= 0.0) ? slope : 0.0;
+}
+
+// Limited slope with its branch as a decision code (BM as in Br): minmod
+// code = 0 (0*SL), 1 (ratio*SL), 2 (SL); moncen code = bit 0 zero slope,
+// bits 1-2 sign of the centred slope (0, +, -), bits 3-4 the minimum taken
+// (1: left, 2: right, 3: centred), bits 5-6 the sign inside its |.|.
+__device__ __forceinline__ int sign_code(double x) { return (x > 0.0) ? 1 : ((x < 0.0) ? 2 : 0); }
+__device__ __forceinline__ double code_sign(int c) { return c == 1 ? 1.0 : (c == 2 ? -1.0 : 0.0); }
+template <int BM>
+__device__ __forceinline__ double limiter_br(int limiter, double SL, double SR, double hl, double hr, double hm,
+                                             unsigned char* code) {
+  if (limiter == LIM_MINMOD) {
+    if (BM == 2) {
+      const int c = *code;
+      if (c == 1) return (SR / SL) * SL;
+      return (c == 2 ? 1.0 : 0.0) * SL;
+    }
+    const double v = minmod(SL, SR);
+    if (BM == 1) {
+      const double r = SR / SL;
+      *code = (unsigned char)((r < 1.0) ? ((r > 0.0) ? 1 : 0) : 2);
+    }
+    return v;
+  }
+  const double dUC = (hl * SL + hr * SR) / (hl + hr);
+  const double q1 = 2.0 * SL * hl / hm, q2 = 2.0 * SR * hr / hm;
+  if (BM == 2) {
+    const int c = *code;
+    if (c & 1) return 0.0;
+    const int sel = (c >> 3) & 3;
+    const double q = sel == 1 ? q1 : (sel == 2 ? q2 : dUC);
+    return code_sign((c >> 1) & 3) * (code_sign((c >> 5) & 3) * q);
+  }
+  const double v = moncen(SL, SR, hl, hr, hm);
+  if (BM == 1) {
+    const double c1 = fabs(q1), c2 = fabs(q2), c3 = fabs(dUC);
+    const double m12 = np_min(c1, c2);
+    const int sel12 = (c1 <= c2 || c1 != c1) ? 1 : 2;
+    const int sel = (m12 <= c3 || m12 != m12) ? sel12 : 3;
+    const double q = sel == 1 ? q1 : (sel == 2 ? q2 : dUC);
+    const int zero = (SL * SR >= 0.0) ? 0 : 1;
+    *code = (unsigned char)(zero | (sign_code(dUC) << 1) | (sel << 3) | (sign_code(q) << 5));
+  }
+  return v;
 }
 
 }  // namespace spd

@@ -364,7 +364,9 @@ __global__ void k_blend_last(Geo g, int d, const double* __restrict__ in, double
 }
 
 // affected faces of direction d (src/trouble_detection.py:81-87) and the
-// marks for the fallback fluxes and the corrected update.
+// marks for the fallback fluxes and the corrected update.  With theta ==
+// nullptr the affected faces already in ``aff`` are used (replayed
+// decisions).
 template <int D>
 __global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__ theta, double* __restrict__ aff,
                            unsigned char* __restrict__ mark_cell, unsigned char* __restrict__ mark_q,
@@ -389,8 +391,13 @@ __global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__
     e2[d] = f[d] + 2;
     const long long i1 = e1[0] + (long long)g.Xe[0] * (e1[1] + (long long)g.Xe[1] * e1[2]);
     const long long i2 = e2[0] + (long long)g.Xe[0] * (e2[1] + (long long)g.Xe[1] * e2[2]);
-    const double a = np_max(theta[i1], theta[i2]);
-    aff[fidx] = a;
+    double a;
+    if (theta) {
+      a = np_max(theta[i1], theta[i2]);
+      aff[fidx] = a;
+    } else {
+      a = aff[fidx];
+    }
     need = godunov || (a != 0.0);
     if (need) {
       mark_cell[i1] = 1;
@@ -427,10 +434,11 @@ static __global__ void k_compact(long long total, const unsigned char* __restric
 
 // MUSCL-Hancock: limited gradients, slopes and the half-step primitive
 // predictor of one extended subcell (src/muscl.py:61-75,129-173,175-216).
-template <int D>
+template <int D, int BM = 0>
 __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __restrict__ dt_ptr, double w_i,
                               const long long* __restrict__ list, const unsigned long long* __restrict__ count,
-                              const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S) {
+                              const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S,
+                              unsigned char* ltape = nullptr) {
   constexpr int V = D + 2, P_ = D + 1;
   const unsigned long long cnt = *count;
   const double dti = *dt_ptr * w_i;
@@ -452,7 +460,9 @@ __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __rest
       const double* M = W_ext + (long long)v * g.Nqe;
       const double SL = (M[e] - M[e - st]) / hl;
       const double SR = (M[e + st] - M[e]) / hr;
-      const double dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
+      double dm;
+      if (BM == 0) dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
+      else dm = limiter_br<BM>(limiter, SL, SR, hl, hr, hm, &ltape[((long long)d * V + v) * g.Nqe + e]);
       dMh[d][v] = dm;
       S[((long long)d * V + v) * g.Nqe + e] = 0.5 * dm * hm;
     }
@@ -478,10 +488,10 @@ __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __rest
 
 // fallback Riemann flux on the affected faces of direction d
 // (src/muscl.py:217-221, src/fv_simulator.py:88-165)
-template <int D>
+template <int D, int BM = 0>
 __global__ void k_muscl_faces(Geo g, int d, int solver, int godunov, const double* __restrict__ aff,
                               const double* __restrict__ Mpred, const double* __restrict__ S,
-                              double* __restrict__ F_FB) {
+                              double* __restrict__ F_FB, unsigned* ftape = nullptr) {
   constexpr int V = D + 2;
   const long long nf = n_faces(g, d);
   const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -505,7 +515,10 @@ __global__ void k_muscl_faces(Geo g, int d, int solver, int godunov, const doubl
     ML[v] = Mpred[(long long)v * g.Nqe + i1] + S[((long long)d * V + v) * g.Nqe + i1];
     MR[v] = Mpred[(long long)v * g.Nqe + i2] - S[((long long)d * V + v) * g.Nqe + i2];
   }
-  riemann<D>(solver, ML, MR, F, g.gamma, g.min_c2, d, true);
+  Br<BM> br;
+  if (BM == 2) br.w = ftape[fidx];
+  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, true, &br);
+  if (BM == 1) ftape[fidx] = br.w;
 #pragma unroll
   for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = F[v];
 }

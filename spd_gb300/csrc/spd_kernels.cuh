@@ -108,13 +108,25 @@ __global__ void k_traces_sp(Ops op, Geo g, const double* __restrict__ U_sp, doub
   write_traces<D, P>(op, g, U_sp, 1, 0, c, tr, 0);
 }
 
+// traces of every (cell, time node) of an iterate U (Tu time nodes stored)
+template <int D, int P>
+__global__ void k_traces_ader(Ops op, Geo g, const double* __restrict__ U, int Tu, int Teff, double* t0, double* t1,
+                              double* t2) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= g.Nc * Teff) return;
+  const long long c = tid % g.Nc;
+  const int t = (int)(tid / g.Nc);
+  double* tr[3] = {t0, t1, t2};
+  write_traces<D, P>(op, g, U, Tu, (Tu == 1) ? 0 : t, c, tr, t);
+}
+
 // ---------------------------------------------------------------------------
 // element-interface Riemann fluxes for direction d
 // (src/sdader_simulator.py:225-234, src/sd_boundary.py:7-76)
 // ---------------------------------------------------------------------------
-template <int D, int P>
+template <int D, int P, int BM = 0>
 __global__ void k_riemann_sd(Geo g, int d, int Teff, int solver, const double* __restrict__ trace,
-                             const double* __restrict__ bcfix, double* __restrict__ Fi) {
+                             const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape = nullptr) {
   using k = K<D, P>;
   const long long nI = n_iface(g, d);
   const long long total = (long long)Teff * k::NJ * nI;
@@ -194,7 +206,10 @@ __global__ void k_riemann_sd(Geo g, int d, int Teff, int solver, const double* _
     }
   }
   double F[k::V];
-  riemann<D>(solver, ML, MR, F, g.gamma, g.min_c2, d, false);
+  Br<BM> br;
+  if (BM == 2) br.w = tape[tid];
+  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, false, &br);
+  if (BM == 1) tape[tid] = br.w;
 #pragma unroll
   for (int v = 0; v < k::V; ++v) Fi[(((long long)v * g.T + t) * k::NJ + j) * nI + iface] = F[v];
 }

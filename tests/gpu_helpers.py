@@ -6,6 +6,17 @@ import numpy as np
 DIMS = ("x", "y", "z")
 
 
+def product_from_golden(data, kw, meta):
+    """The product simulator with a golden case's constants and initial state."""
+    from golden_cases import golden_operators, make_ic
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(init_fct=make_ic(meta["ic"]), operators=golden_operators(data), verbose=False, **kw)
+    s.dm.U_sp = data["init_U_sp"]
+    s.dm.U_cv = data["init_U_cv"]
+    s.dm.W_cv = data["init_W_cv"]
+    return s
+
+
 def oracle_like(s, **override):
     """An oracle run with the same constants and initial state as the
     product simulator ``s`` (state downloaded from the device)."""

@@ -6,19 +6,10 @@ specification are implied."""
 import numpy as np
 import pytest
 
-from golden_cases import DIMS, case_names, golden_operators, load, make_ic
-from gpu_helpers import compare, oracle_like, step_both
+from golden_cases import DIMS, case_names, load
+from gpu_helpers import compare, oracle_like, product_from_golden, step_both
 
 pytestmark = pytest.mark.gpu
-
-
-def product_from_golden(data, kw, meta):
-    from spd_gb300 import SDADER_Simulator
-    s = SDADER_Simulator(init_fct=make_ic(meta["ic"]), operators=golden_operators(data), verbose=False, **kw)
-    s.dm.U_sp = data["init_U_sp"]
-    s.dm.U_cv = data["init_U_cv"]
-    s.dm.W_cv = data["init_W_cv"]
-    return s
 
 
 @pytest.mark.parametrize("name", case_names())
