@@ -37,6 +37,10 @@ WORKLOADS = {
     "sedov128": "3D Sedov blast, 128^3 cells, p=2, FV update with limiting, HLLC, reflective",
     "kh_ensemble": "batched: 64 periodic Kelvin-Helmholtz shear layers, p=3, sides drawn from "
                    "{64,128,192,256,384,512} (seed 2026), HLLC + limiting, per-instance dt",
+    "kh_adjoint": "gradient of J = ||rho(T) - rho_target||^2 with respect to the initial density, periodic "
+                  "Kelvin-Helmholtz shear layer, 256x256 cells, p=3, 200 steps, HLLC + limiting (masks, "
+                  "branches and dt frozen from the forward), sqrt(N) checkpoints; rho_target from a forward run "
+                  "of a seeded 1e-2 Gaussian density perturbation",
 }
 
 
@@ -408,6 +412,88 @@ def ensemble_arm(args):
         s.close()
 
 
+def adjoint_arm(args):
+    """Forward and backward (adjoint) time of the KH gradient; the headline
+    value is gradients/s, with the backward/forward time ratio beside it."""
+    import numpy as np
+    import torch
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.adjoint import AdjointRunner
+    from spd_gb300.initial_conditions import kelvin_helmholtz
+    n = args.cells or 256
+    nsteps = args.adj_steps
+
+    def make():
+        return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=7), update="FV", FB=True,
+                                riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                BC=(("periodic", "periodic"),) * 2, verbose=False)
+
+    s = make()
+    U0 = torch.tensor(s.dm.U_sp, device="cuda")
+    shape = tuple(U0.shape)
+    rng = np.random.default_rng(2027)
+    Ut = U0.clone()
+    Ut[0] = U0[0] * (1.0 + 1e-2 * torch.tensor(rng.standard_normal(shape[1:]), device="cuda"))
+    target = AdjointRunner(s, nsteps).forward(Ut)[0].clone()
+
+    # plain forward (the step loop without checkpoints) for the cost ratio
+    s.dm.U_sp = U0.cpu().numpy()
+    s._ctx.end_sim()
+    for _ in range(args.warmup):
+        s.compute_dt()
+        s.perform_update()
+    s.dm.U_sp = U0.cpu().numpy()
+    s._ctx.end_sim()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.time, done = s._ctx.step(nsteps, 0.0, 0, s.time)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    results = []
+    with ClockSampler() as clk:
+        for rep in range(max(1, args.steps)):
+            r = AdjointRunner(s, nsteps)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            y = r.forward(U0)
+            res = y[0] - target
+            J = float((res * res).sum())
+            gy = torch.zeros_like(y)
+            gy[0] = 2.0 * res
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            g = r.backward(gy)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            results.append((t1 - t0, t2 - t1))
+    fwd_s = min(a for a, _ in results)
+    bwd_s = min(b for _, b in results)
+    grad_rho = g[0]
+    # per-kernel device time of one more forward + backward (CUDA events)
+    s._ctx.profile(True)
+    r = AdjointRunner(s, nsteps)
+    y = r.forward(U0)
+    fwd_prof = s._ctx.profile_report()
+    r.backward(gy)
+    bwd_prof = s._ctx.profile_report()
+    s._ctx.profile(False)
+    top = sorted(bwd_prof.items(), key=lambda kv: -kv[1][1])[:10]
+    line = {"metric": "gradients/s (KH 256^2, p=3, 200 steps, FP64 adjoint)", "value": 1.0 / (fwd_s + bwd_s),
+            "unit": "gradients/s", "n_gpus": 1, "steps": len(results), "warmup": args.warmup,
+            "ms_per_step": (fwd_s + bwd_s) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["kh_adjoint"], "cells": [n, n], "time_steps": nsteps,
+                       "checkpoint_every": r.k},
+            "forward_plain_s": plain_s, "forward_with_checkpoints_s": fwd_s, "backward_s": bwd_s,
+            "backward_over_forward": bwd_s / plain_s, "J": J,
+            "grad_rho_norm": float(torch.linalg.vector_norm(grad_rho)), "clocks": clk.summary(),
+            "forward_kernels_ms": round(sum(v[1] for v in fwd_prof.values()), 3),
+            "backward_kernels_ms": round(sum(v[1] for v in bwd_prof.values()), 3),
+            "backward_top_kernels_ms": {k: [v[0], round(v[1], 3)] for k, v in top}}
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -419,6 +505,7 @@ def main():
     ap.add_argument("--instances", type=int, default=64, help="ensemble size (kh_ensemble)")
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per direction (a smaller case of the workload, for profiling)")
+    ap.add_argument("--adj-steps", type=int, default=200, help="time steps of the differentiated run (kh_adjoint)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -426,6 +513,10 @@ def main():
         from spd_gb300.build import build
         build()
         ensemble_arm(args)
+    elif args.workload == "kh_adjoint":
+        from spd_gb300.build import build
+        build()
+        adjoint_arm(args)
     else:
         from spd_gb300.build import build
         if int(os.environ.get("LOCAL_RANK", "0")) == 0:

@@ -3,82 +3,16 @@
 // blending weights theta, the minmod branches and the Riemann-solver
 // branches frozen at their forward values.  Linear pieces (interpolation,
 // derivative, Picard sums, subcell transforms, flux divergence, boundary
-// copies) are transposed directly; the local nonlinear maps (primitives,
-// Euler flux, LLF/HLLC, the MUSCL-Hancock predictor) use forward-mode dual
-// numbers over their few inputs to form J^T * adjoint.  Adjoint arrays use
-// the forward layouts (spd_kernels.cuh, spd_fv.cuh); suffix _a.
+// copies) are transposed directly; the pointwise nonlinear maps
+// (primitives, Euler flux, LLF/HLLC) use the reverse-mode products of
+// spd_vjp.cuh, and the MUSCL-Hancock half-step predictor forward-mode dual
+// numbers over its inputs.  Adjoint arrays use the forward layouts
+// (spd_kernels.cuh, spd_fv.cuh); suffix _a.
 #pragma once
 #include "spd_fv.cuh"
+#include "spd_vjp.cuh"
 
 namespace spd {
-
-// ---------------------------------------------------------------------------
-// local vector-Jacobian products
-// ---------------------------------------------------------------------------
-// W = prim(U): Ua = (dW/dU)^T Wa
-template <int D>
-__device__ __forceinline__ void prim_vjp(const double* U, const double* Wa, double* Ua, double gamma) {
-  constexpr int V = D + 2;
-  Dual<V> u[V], w[V];
-#pragma unroll
-  for (int i = 0; i < V; ++i) {
-    u[i] = Dual<V>(U[i]);
-    u[i].d[i] = 1.0;
-  }
-  prim<D>(u, w, gamma, 0);
-#pragma unroll
-  for (int i = 0; i < V; ++i) {
-    double s = 0.0;
-#pragma unroll
-    for (int v = 0; v < V; ++v) s += Wa[v] * w[v].d[i];
-    Ua[i] = s;
-  }
-}
-
-// F = flux(prim(M)) in direction d (interior flux points)
-template <int D>
-__device__ __forceinline__ void fpflux_vjp(const double* M, const double* Fa, double* Ma, double gamma, int d) {
-  constexpr int V = D + 2;
-  Dual<V> m[V], w[V], f[V];
-#pragma unroll
-  for (int i = 0; i < V; ++i) {
-    m[i] = Dual<V>(M[i]);
-    m[i].d[i] = 1.0;
-  }
-  prim<D>(m, w, gamma, 0);
-  flux<D>(w, f, gamma, d);
-#pragma unroll
-  for (int i = 0; i < V; ++i) {
-    double s = 0.0;
-#pragma unroll
-    for (int v = 0; v < V; ++v) s += Fa[v] * f[v].d[i];
-    Ma[i] = s;
-  }
-}
-
-// F = riemann(ML, MR): (MLa, MRa) = J^T Fa
-template <int D>
-__device__ __forceinline__ void riemann_vjp(int solver, const double* ML, const double* MR, const double* Fa,
-                                            double* MLa, double* MRa, double gamma, double min_c2, int d, bool prims) {
-  constexpr int V = D + 2;
-  Dual<2 * V> l[V], r[V], f[V];
-#pragma unroll
-  for (int i = 0; i < V; ++i) {
-    l[i] = Dual<2 * V>(ML[i]);
-    l[i].d[i] = 1.0;
-    r[i] = Dual<2 * V>(MR[i]);
-    r[i].d[V + i] = 1.0;
-  }
-  riemann<D>(solver, l, r, f, gamma, min_c2, d, prims);
-#pragma unroll
-  for (int i = 0; i < 2 * V; ++i) {
-    double s = 0.0;
-#pragma unroll
-    for (int v = 0; v < V; ++v) s += Fa[v] * f[v].d[i];
-    if (i < V) MLa[i] = s;
-    else MRa[i - V] = s;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // predictor
@@ -149,7 +83,14 @@ __global__ void k_adj_interior(Ops op, Geo g, int mode, int Teff, const double* 
           M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
           Fa[v] = Fla[v][f];
         }
-        fpflux_vjp<D>(M, Fa, Ma, g.gamma, d);
+        {
+          double W[k::V], Wa[k::V];
+          prim<D>(M, W, g.gamma, 0);
+#pragma unroll
+          for (int v = 0; v < k::V; ++v) { Wa[v] = 0.0; Ma[v] = 0.0; }
+          flux_vjp_add<D>(W, Fa, Wa, g.gamma, d);
+          prim_vjp_add<D>(M, Wa, Ma, g.gamma);
+        }
 #pragma unroll
         for (int v = 0; v < k::V; ++v)
 #pragma unroll
@@ -265,7 +206,7 @@ __global__ void k_adj_riemann(Geo g, int d, int Teff, int solver, const double* 
     }
   }
   double MLa[k::V], MRa[k::V];
-  riemann_vjp<D>(solver, ML, MR, Fa, MLa, MRa, g.gamma, g.min_c2, d, false);
+  riemann_vjp_rev<D>(solver, ML, MR, Fa, MLa, MRa, g.gamma, g.min_c2, d, false);
 #pragma unroll
   for (int v = 0; v < k::V; ++v) {
     if (srcL >= 0) atomicAdd(&Tra[tidx(sideL, v, srcL)], (negL && v == d + 1) ? -MLa[v] : MLa[v]);
@@ -620,6 +561,51 @@ __device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg
   for (int v = 0; v < V; ++v) pr[v] = w[v] + 0.5 * dtW[v] * dti;
 }
 
+// The forward's half-step prediction and direction-dd slope term of
+// extended cell e (k_muscl_cells arithmetic, values only).
+template <int D>
+__device__ __forceinline__ void muscl_cell_values(const Geo& g, const FvGeo& fg, int limiter, double dti, long long e,
+                                                  int dsel, const double* __restrict__ W_ext, double* pred,
+                                                  double* Sd) {
+  constexpr int V = D + 2, P_ = D + 1;
+  int c[3];
+  e_coords(g, e, c[0], c[1], c[2]);
+  double W[V], dMh[D][V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) W[v] = W_ext[(long long)v * g.Nqe + e];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const long long st = ext_stride(g, d);
+    const int k = c[d];
+    const double hl = fg.hcv[d][k - 1], hr = fg.hcv[d][k], hm = fg.hfp[d][k];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const double* M = W_ext + (long long)v * g.Nqe;
+      const double SL = (M[e] - M[e - st]) / hl;
+      const double SR = (M[e + st] - M[e]) / hr;
+      const double dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
+      dMh[d][v] = dm;
+      if (d == dsel) Sd[v] = 0.5 * dm * hm;
+    }
+  }
+  double dtW[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) dtW[v] = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int vel = d + 1;
+    const double* dW = dMh[d];
+    dtW[0] = dtW[0] - (W[vel] * dW[0] + W[0] * dW[vel]);
+    dtW[P_] = dtW[P_] - (W[vel] * dW[P_] + g.gamma * W[P_] * dW[vel]);
+    dtW[vel] = dtW[vel] - (W[vel] * dW[vel] + dW[P_] / W[0]);
+#pragma unroll
+    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - W[vel] * dW[v2];
+  }
+  dtW[P_] = dtW[P_] * 0.0;
+#pragma unroll
+  for (int v = 0; v < V; ++v) pred[v] = W[v] + 0.5 * dtW[v] * dti;
+}
+
 // MUSCL-Hancock adjoint, phase 1: on every face of direction d whose
 // fallback flux was used, the Riemann VJP of Fb_a onto the two
 // reconstructed states, FA[side][v][face] (side 0 = left state).
@@ -628,7 +614,7 @@ __global__ void k_adj_muscl_riemann(Geo g, FvGeo fg, int d, int solver, int limi
                                     const double* __restrict__ dt_ptr, double w_i, const double* __restrict__ aff,
                                     const double* __restrict__ W_ext, const double* __restrict__ Fba,
                                     double* __restrict__ FA) {
-  constexpr int V = D + 2, NT = V * (1 + D);
+  constexpr int V = D + 2;
   const long long nf = n_faces(g, d);
   const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (fidx >= nf) return;
@@ -647,18 +633,13 @@ __global__ void k_adj_muscl_riemann(Geo g, FvGeo fg, int d, int solver, int limi
   const double dti = *dt_ptr * w_i;
   double M[2][V];
   for (int side = 0; side < 2; ++side) {
-    double W[V], SLs[D][V], SRs[D][V], dMh[D][V];
-    Dual<NT> pr[V];
-    muscl_cell_forward<D>(g, fg, limiter, dti, ecell[side], W_ext, W, SLs, SRs, dMh, pr);
-    const double hm = fg.hfp[d][e1c[d] + side];
-    for (int v = 0; v < V; ++v) {
-      const double S = 0.5 * dMh[d][v] * hm;
-      M[side][v] = (side == 0) ? pr[v].v + S : pr[v].v - S;
-    }
+    double pred[V], Sd[V];
+    muscl_cell_values<D>(g, fg, limiter, dti, ecell[side], d, W_ext, pred, Sd);
+    for (int v = 0; v < V; ++v) M[side][v] = (side == 0) ? pred[v] + Sd[v] : pred[v] - Sd[v];
   }
   double Fa[V], MLa[V], MRa[V];
   for (int v = 0; v < V; ++v) Fa[v] = Fba[(long long)v * nf + fidx];
-  riemann_vjp<D>(solver, M[0], M[1], Fa, MLa, MRa, g.gamma, g.min_c2, d, true);
+  riemann_vjp_rev<D>(solver, M[0], M[1], Fa, MLa, MRa, g.gamma, g.min_c2, d, true);
   for (int v = 0; v < V; ++v) {
     FA[(long long)v * nf + fidx] = MLa[v];
     FA[(long long)(V + v) * nf + fidx] = MRa[v];
@@ -831,7 +812,11 @@ __global__ void k_adj_prim_cv(Geo g, const double* __restrict__ U_cv, const doub
     W_a[(long long)v * g.Nqe + e] = 0.0;
     any = any || (Wa[v] != 0.0);
   }
-  if (any) prim_vjp<D>(U, Wa, Ua, g.gamma);
+  if (any) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) Ua[v] = 0.0;
+    prim_vjp_add<D>(U, Wa, Ua, g.gamma);
+  }
 #pragma unroll
   for (int v = 0; v < V; ++v)
     Ucv_a[(long long)v * g.Nq + q] = Unew_a[(long long)v * g.Nq + q] + (any ? Ua[v] : 0.0);

@@ -8,6 +8,11 @@
 #include <cstdint>
 #include <cmath>
 
+// device code; also host-callable so the scalar maps can be checked on a CPU
+#ifndef SPD_FN
+#define SPD_FN __host__ __device__ __forceinline__
+#endif
+
 namespace spd {
 
 
@@ -30,84 +35,84 @@ template <int N>
 struct Dual {
   double v;
   double d[N];
-  __device__ __forceinline__ Dual() {}
-  __device__ __forceinline__ Dual(double x) : v(x) {
+  SPD_FN Dual() {}
+  SPD_FN Dual(double x) : v(x) {
 #pragma unroll
     for (int i = 0; i < N; ++i) d[i] = 0.0;
   }
 };
 template <int N>
-__device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r; r.v = a.v + b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
   return r;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r; r.v = a.v - b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
   return r;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
+SPD_FN Dual<N> operator-(const Dual<N>& a) {
   Dual<N> r; r.v = -a.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
   return r;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r; r.v = a.v * b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
   return r;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r; r.v = a.v / b.v;
   const double ib = 1.0 / b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
   return r;
 }
-template <int N> __device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, double b) { return a + Dual<N>(b); }
-template <int N> __device__ __forceinline__ Dual<N> operator+(double a, const Dual<N>& b) { return Dual<N>(a) + b; }
-template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, double b) { return a - Dual<N>(b); }
-template <int N> __device__ __forceinline__ Dual<N> operator-(double a, const Dual<N>& b) { return Dual<N>(a) - b; }
+template <int N> SPD_FN Dual<N> operator+(const Dual<N>& a, double b) { return a + Dual<N>(b); }
+template <int N> SPD_FN Dual<N> operator+(double a, const Dual<N>& b) { return Dual<N>(a) + b; }
+template <int N> SPD_FN Dual<N> operator-(const Dual<N>& a, double b) { return a - Dual<N>(b); }
+template <int N> SPD_FN Dual<N> operator-(double a, const Dual<N>& b) { return Dual<N>(a) - b; }
 template <int N>
-__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, double b) {
+SPD_FN Dual<N> operator*(const Dual<N>& a, double b) {
   Dual<N> r; r.v = a.v * b;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
   return r;
 }
-template <int N> __device__ __forceinline__ Dual<N> operator*(double a, const Dual<N>& b) { return b * a; }
-template <int N> __device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, double b) { return a / Dual<N>(b); }
-template <int N> __device__ __forceinline__ Dual<N> operator/(double a, const Dual<N>& b) { return Dual<N>(a) / b; }
-template <int N> __device__ __forceinline__ bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
-template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
-template <int N> __device__ __forceinline__ bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
-template <int N> __device__ __forceinline__ bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
-template <int N> __device__ __forceinline__ bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
-template <int N> __device__ __forceinline__ bool operator<(const Dual<N>& a, double b) { return a.v < b; }
-template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, double b) { return a.v > b; }
+template <int N> SPD_FN Dual<N> operator*(double a, const Dual<N>& b) { return b * a; }
+template <int N> SPD_FN Dual<N> operator/(const Dual<N>& a, double b) { return a / Dual<N>(b); }
+template <int N> SPD_FN Dual<N> operator/(double a, const Dual<N>& b) { return Dual<N>(a) / b; }
+template <int N> SPD_FN bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
+template <int N> SPD_FN bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
+template <int N> SPD_FN bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
+template <int N> SPD_FN bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
+template <int N> SPD_FN bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
+template <int N> SPD_FN bool operator<(const Dual<N>& a, double b) { return a.v < b; }
+template <int N> SPD_FN bool operator>(const Dual<N>& a, double b) { return a.v > b; }
 
-__device__ __forceinline__ double sval(double x) { return x; }
-template <int N> __device__ __forceinline__ double sval(const Dual<N>& x) { return x.v; }
-__device__ __forceinline__ double ad_sqrt(double x) { return sqrt(x); }
+SPD_FN double sval(double x) { return x; }
+template <int N> SPD_FN double sval(const Dual<N>& x) { return x.v; }
+SPD_FN double ad_sqrt(double x) { return sqrt(x); }
 template <int N>
-__device__ __forceinline__ Dual<N> ad_sqrt(const Dual<N>& x) {
+SPD_FN Dual<N> ad_sqrt(const Dual<N>& x) {
   Dual<N> r; r.v = sqrt(x.v);
   const double k = 0.5 / r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
   return r;
 }
-__device__ __forceinline__ double ad_abs(double x) { return fabs(x); }
+SPD_FN double ad_abs(double x) { return fabs(x); }
 template <int N>
-__device__ __forceinline__ Dual<N> ad_abs(const Dual<N>& x) {
+SPD_FN Dual<N> ad_abs(const Dual<N>& x) {
   if (x.v > 0) return x;
   if (x.v < 0) return -x;
   return Dual<N>(fabs(x.v));
@@ -115,14 +120,14 @@ __device__ __forceinline__ Dual<N> ad_abs(const Dual<N>& x) {
 
 // NumPy's maximum / minimum: NaN in either argument propagates.
 template <class S>
-__device__ __forceinline__ S np_max(const S& a, const S& b) { return (a >= b || a != a) ? a : b; }
+SPD_FN S np_max(const S& a, const S& b) { return (a >= b || a != a) ? a : b; }
 template <class S>
-__device__ __forceinline__ S np_min(const S& a, const S& b) { return (a <= b || a != a) ? a : b; }
+SPD_FN S np_min(const S& a, const S& b) { return (a <= b || a != a) ? a : b; }
 // Dual forms: same value; at a tie the derivative is the mean of the two
 // arguments' derivatives (the subgradient torch.maximum / torch.minimum
 // propagate).
 template <int N>
-__device__ __forceinline__ Dual<N> tie_mean(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> tie_mean(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r;
   r.v = a.v;
 #pragma unroll
@@ -130,12 +135,12 @@ __device__ __forceinline__ Dual<N> tie_mean(const Dual<N>& a, const Dual<N>& b) 
   return r;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> np_max(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> np_max(const Dual<N>& a, const Dual<N>& b) {
   if (a.v == b.v) return tie_mean(a, b);
   return (a.v >= b.v || a.v != a.v) ? a : b;
 }
 template <int N>
-__device__ __forceinline__ Dual<N> np_min(const Dual<N>& a, const Dual<N>& b) {
+SPD_FN Dual<N> np_min(const Dual<N>& a, const Dual<N>& b) {
   if (a.v == b.v) return tie_mean(a, b);
   return (a.v <= b.v || a.v != a.v) ? a : b;
 }
@@ -152,7 +157,7 @@ struct Br {
   int k = 0;
 };
 template <int BM>
-__device__ __forceinline__ bool pick(Br<BM>* br, bool live) {
+SPD_FN bool pick(Br<BM>* br, bool live) {
   if (BM == 0) return live;
   if (BM == 1) {
     if (live) br->w |= (1u << br->k);
@@ -165,7 +170,7 @@ __device__ __forceinline__ bool pick(Br<BM>* br, bool live) {
 }
 // |x| whose sign is a recorded decision under BM != 0
 template <int BM, class S>
-__device__ __forceinline__ S abs_br(const S& x, Br<BM>* br) {
+SPD_FN S abs_br(const S& x, Br<BM>* br) {
   if (BM == 0) return ad_abs(x);
   return pick(br, sval(x) >= 0.0) ? x : -x;
 }
@@ -173,13 +178,13 @@ __device__ __forceinline__ S abs_br(const S& x, Br<BM>* br) {
 // Velocity index k (0-based) of the rotated frame used for direction idim:
 // np.roll(vels, -idim) (src/sdader_simulator.py:219).
 template <int D>
-__device__ __forceinline__ int rvel(int idim, int k) { return 1 + (idim + k) % D; }
+SPD_FN int rvel(int idim, int k) { return 1 + (idim + k) % D; }
 
 // U -> W (src/hydro.py:48-86); the kinetic term sums in the order of the
 // velocity list, which is the rotated list inside the Riemann wrapper
 // (src/riemann_solver.py:10-29) and the plain list elsewhere.
 template <int D, class S>
-__device__ __forceinline__ void prim(const S* U, S* W, double gamma, int idim_order) {
+SPD_FN void prim(const S* U, S* W, double gamma, int idim_order) {
   constexpr int P_ = D + 1;
   W[0] = U[0];
   S K = 0.0;
@@ -196,7 +201,7 @@ __device__ __forceinline__ void prim(const S* U, S* W, double gamma, int idim_or
 
 // W -> U (src/hydro.py:88-125).
 template <int D, class S>
-__device__ __forceinline__ void cons(const S* W, S* U, double gamma, int idim_order) {
+SPD_FN void cons(const S* W, S* U, double gamma, int idim_order) {
   constexpr int P_ = D + 1;
   U[0] = W[0];
   S K = 0.0;
@@ -213,7 +218,7 @@ __device__ __forceinline__ void cons(const S* W, S* U, double gamma, int idim_or
 
 // Euler flux in the rotated frame of direction idim (src/hydro.py:127-170).
 template <int D, class S>
-__device__ __forceinline__ void flux(const S* W, S* F, double gamma, int idim) {
+SPD_FN void flux(const S* W, S* F, double gamma, int idim) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
   S K = 0.0, m = 0.0;
@@ -233,7 +238,7 @@ __device__ __forceinline__ void flux(const S* W, S* F, double gamma, int idim) {
 
 // Sound speed with floor (src/hydro.py:3-46).
 template <class S, int BM = 0>
-__device__ __forceinline__ S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
+SPD_FN S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
                                          Br<BM>* br = nullptr) {
   S c2 = gamma * P / rho;
   c2 = pick(br, c2 > min_c2) ? c2 : S(min_c2);
@@ -242,7 +247,7 @@ __device__ __forceinline__ S sound_speed(const S& P, const S& rho, double gamma,
 
 // LLF (src/riemann_solver.py:31-65).
 template <int D, class S, int BM = 0>
-__device__ __forceinline__ void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
+SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
                                     double min_c2, int idim, Br<BM>* br = nullptr) {
   constexpr int V = D + 2, P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
@@ -260,7 +265,7 @@ __device__ __forceinline__ void llf(const S* WL, const S* WR, const S* UL, const
 // HLLC (src/riemann_solver.py:67-145) and its low-Mach variant (:147-212).
 // Only the branch the reference's np.where chain selects is evaluated.
 template <int D, class S, int BM = 0>
-__device__ __forceinline__ void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
+SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
                                      double min_c2, int idim, bool low_mach, Br<BM>* br = nullptr) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
@@ -322,7 +327,7 @@ __device__ __forceinline__ void hllc(const S* WL, const S* WR, const S* UL, cons
 // Riemann wrapper (src/riemann_solver.py:10-29): inputs conservative
 // (prims=false) or primitive (prims=true); rotated velocity order.
 template <int D, class S, int BM = 0>
-__device__ __forceinline__ void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, double min_c2,
+SPD_FN void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, double min_c2,
                                         int idim, bool prims, Br<BM>* br = nullptr) {
   constexpr int V = D + 2;
   S WL[V], WR[V], UL[V], UR[V];
@@ -346,14 +351,14 @@ __device__ __forceinline__ void riemann(int solver, const S* ML, const S* MR, S*
 // accumulated separately, then added); otherwise a left-to-right sum
 // (src/transforms.py:3-25).
 template <int L>
-__device__ __forceinline__ double dot_seq(const double* A, const double* x) {
+SPD_FN double dot_seq(const double* A, const double* x) {
   double acc = A[0] * x[0];
 #pragma unroll
   for (int s = 1; s < L; ++s) acc = acc + A[s] * x[s];
   return acc;
 }
 template <int L>
-__device__ __forceinline__ double dot_lanes2(const double* A, const double* x) {
+SPD_FN double dot_lanes2(const double* A, const double* x) {
   double e = A[0] * x[0];
   if (L == 1) return e;
   double o = A[1] * x[1];
@@ -365,20 +370,20 @@ __device__ __forceinline__ double dot_lanes2(const double* A, const double* x) {
   return e + o;
 }
 template <int L>
-__device__ __forceinline__ double dot_dir(const double* A, const double* x, int idim) {
+SPD_FN double dot_dir(const double* A, const double* x, int idim) {
   return idim == 0 ? dot_lanes2<L>(A, x) : dot_seq<L>(A, x);
 }
 
 // Limiters (src/muscl.py:12-59); NaN semantics follow the np.where forms.
-__device__ __forceinline__ double minmod(double SL, double SR) {
+SPD_FN double minmod(double SL, double SR) {
   double r = SR / SL;
   r = (r < 1.0) ? r : 1.0;
   return ((r > 0.0) ? r : 0.0) * SL;
 }
-__device__ __forceinline__ double np_sign(double x) {
+SPD_FN double np_sign(double x) {
   return (x > 0.0) ? 1.0 : ((x < 0.0) ? -1.0 : ((x == 0.0) ? 0.0 : x));
 }
-__device__ __forceinline__ double moncen(double dUL, double dUR, double dxL, double dxR, double dxM) {
+SPD_FN double moncen(double dUL, double dUR, double dxL, double dxR, double dxM) {
   const double dUC = (dxL * dUL + dxR * dUR) / (dxL + dxR);
   double slope = np_min(fabs(2.0 * dUL * dxL / dxM), fabs(2.0 * dUR * dxR / dxM));
   slope = np_sign(dUC) * np_min(slope, fabs(dUC));
@@ -389,10 +394,10 @@ __device__ __forceinline__ double moncen(double dUL, double dUR, double dxL, dou
 // code = 0 (0*SL), 1 (ratio*SL), 2 (SL); moncen code = bit 0 zero slope,
 // bits 1-2 sign of the centred slope (0, +, -), bits 3-4 the minimum taken
 // (1: left, 2: right, 3: centred), bits 5-6 the sign inside its |.|.
-__device__ __forceinline__ int sign_code(double x) { return (x > 0.0) ? 1 : ((x < 0.0) ? 2 : 0); }
-__device__ __forceinline__ double code_sign(int c) { return c == 1 ? 1.0 : (c == 2 ? -1.0 : 0.0); }
+SPD_FN int sign_code(double x) { return (x > 0.0) ? 1 : ((x < 0.0) ? 2 : 0); }
+SPD_FN double code_sign(int c) { return c == 1 ? 1.0 : (c == 2 ? -1.0 : 0.0); }
 template <int BM>
-__device__ __forceinline__ double limiter_br(int limiter, double SL, double SR, double hl, double hr, double hm,
+SPD_FN double limiter_br(int limiter, double SL, double SR, double hl, double hr, double hm,
                                              unsigned char* code) {
   if (limiter == LIM_MINMOD) {
     if (BM == 2) {
