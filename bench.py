@@ -423,8 +423,8 @@ def adjoint_arm(args):
     n = args.cells or 256
     nsteps = args.adj_steps
 
-    def make():
-        return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=7), update="FV", FB=True,
+    def make(seed=7):
+        return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=seed), update="FV", FB=True,
                                 riemann_solver_sd="hllc", riemann_solver_fv="hllc",
                                 BC=(("periodic", "periodic"),) * 2, verbose=False)
 
@@ -490,8 +490,99 @@ def adjoint_arm(args):
             "forward_kernels_ms": round(sum(v[1] for v in fwd_prof.values()), 3),
             "backward_kernels_ms": round(sum(v[1] for v in bwd_prof.values()), 3),
             "backward_top_kernels_ms": {k: [v[0], round(v[1], 3)] for k, v in top}}
+    if args.fd_dirs:
+        line["fd_check"] = adjoint_fd_check(s, U0, target, r.dts, g, args.fd_dirs)
+    if args.batch > 1:
+        line["batch"] = adjoint_batch(args, make_batch=lambda i: make(seed=100 + i), n=n, nsteps=nsteps)
     print(json.dumps(line), flush=True)
     s.close()
+
+
+def adjoint_fd_check(s, U0, target, dts, g, ndirs, eps=1e-6, seed=2028):
+    """Central differences of J along seeded density-only directions
+    (entrywise relative to the density) against the adjoint gradient.  The
+    perturbed runs replay the forward's dts and every decision (affected
+    faces, Riemann-solver and limiter branches) from decision tapes, so
+    both sides see the same frozen-decision map."""
+    import numpy as np
+    import torch
+    ctx = s._ctx
+    nsteps = len(dts)
+    shape = tuple(U0.shape)
+    count = U0.numel()
+    ctx.tape_enable(nsteps)
+
+    def put(x):
+        x = x.contiguous()
+        torch.cuda.synchronize()
+        ctx.upload_ptr("U_sp", x.data_ptr(), count)
+
+    def run(mode):
+        for j in range(nsteps):
+            ctx.tape_step(j, dts[j], mode)
+        y = torch.empty(shape, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        ctx.download_ptr("U_sp", y.data_ptr(), count)
+        res = y[0] - target
+        return float((res * res).sum())
+
+    put(U0)
+    J0 = run(1)
+    put(U0)
+    J0r = run(2)
+    rng = np.random.default_rng(seed)
+    errs = []
+    t0 = time.perf_counter()
+    for _ in range(ndirs):
+        v = torch.zeros_like(U0)
+        v[0] = torch.tensor(rng.standard_normal(shape[1:]), device="cuda") * U0[0].abs()
+        put(U0 + eps * v)
+        Jp = run(2)
+        put(U0 - eps * v)
+        Jm = run(2)
+        fd = (Jp - Jm) / (2 * eps)
+        ad = float((g * v).sum())
+        errs.append(abs(fd - ad) / abs(ad))
+    return {"directions": ndirs, "eps_relative": eps, "replay_reproduces_forward": J0 == J0r,
+            "median_rel_err": float(np.median(errs)), "max_rel_err": float(np.max(errs)),
+            "rel_errs": [float("%.3e" % e) for e in errs], "seconds": time.perf_counter() - t0}
+
+
+def adjoint_batch(args, make_batch, n, nsteps):
+    """B seeded instances (own targets), each gradient on its own context and
+    stream, driven by one host thread per instance."""
+    import concurrent.futures
+    import numpy as np
+    import torch
+    from spd_gb300.adjoint import AdjointRunner
+    B = args.batch
+    sims = [make_batch(i) for i in range(B)]
+    U0s = [torch.tensor(sm.dm.U_sp, device="cuda") for sm in sims]
+    targets = []
+    for i, sm in enumerate(sims):
+        rng = np.random.default_rng(3000 + i)
+        Ut = U0s[i].clone()
+        Ut[0] = U0s[i][0] * (1.0 + 1e-2 * torch.tensor(rng.standard_normal(tuple(Ut.shape[1:])), device="cuda"))
+        targets.append(AdjointRunner(sm, nsteps).forward(Ut)[0].clone())
+    torch.cuda.synchronize()
+
+    def one(i):
+        r = AdjointRunner(sims[i], nsteps)
+        y = r.forward(U0s[i])
+        res = y[0] - targets[i]
+        gy = torch.zeros_like(y)
+        gy[0] = 2.0 * res
+        g = r.backward(gy)
+        return float(torch.linalg.vector_norm(g[0]))
+
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=B) as ex:
+        norms = list(ex.map(one, range(B)))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    for sm in sims:
+        sm.close()
+    return {"instances": B, "wall_s": wall, "gradients_per_s": B / wall, "grad_rho_norms": norms}
 
 
 def main():
@@ -506,6 +597,8 @@ def main():
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per direction (a smaller case of the workload, for profiling)")
     ap.add_argument("--adj-steps", type=int, default=200, help="time steps of the differentiated run (kh_adjoint)")
+    ap.add_argument("--fd-dirs", type=int, default=0, help="central-difference directions to check (kh_adjoint)")
+    ap.add_argument("--batch", type=int, default=1, help="seeded instances run concurrently (kh_adjoint)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

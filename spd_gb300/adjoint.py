@@ -30,9 +30,11 @@ import torch
 __all__ = ["SDADERSteps", "AdjointRunner", "run_steps"]
 
 
-def _sync():
-    if torch.cuda.is_available():
-        torch.cuda.synchronize()
+def _sync(t: torch.Tensor):
+    """Wait for the work queued on ``t``'s device by this thread's current
+    torch stream (the library's own stream is synchronised by each call)."""
+    if t.is_cuda:
+        torch.cuda.current_stream(t.device).synchronize()
 
 
 class AdjointRunner:
@@ -71,12 +73,12 @@ class AdjointRunner:
         x = x.detach().to(torch.float64).contiguous()
         if tuple(x.shape) != tuple(self.shape):
             raise ValueError(f"{field}: expected shape {self.shape}, got {tuple(x.shape)}")
-        _sync()
+        _sync(x)
         self.ctx.upload_ptr(field, x.data_ptr(), self.count)
 
     def _get(self, field: str, device=None) -> torch.Tensor:
         out = torch.empty(self.shape, dtype=torch.float64, device=device or self.device)
-        _sync()
+        _sync(out)
         self.ctx.download_ptr(field, out.data_ptr(), self.count)
         return out
 
