@@ -7,6 +7,7 @@
 #pragma once
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 // device code; also host-callable so the scalar maps can be checked on a CPU
 #ifndef SPD_FN
@@ -99,6 +100,29 @@ template <int N> SPD_FN bool operator!=(const Dual<N>& a, const Dual<N>& b) { re
 template <int N> SPD_FN bool operator<(const Dual<N>& a, double b) { return a.v < b; }
 template <int N> SPD_FN bool operator>(const Dual<N>& a, double b) { return a.v > b; }
 
+// Correctly rounded a / b from a correctly rounded reciprocal rb = RN(1/b)
+// (b finite and nonzero) by Markstein's correction (P. Markstein, IBM J.
+// Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, 2nd ed., Thm. 5.3): q = RN(a*rb) is within one ulp of a/b, the
+// residual a - b*q is exact in one fused multiply-add, and RN(q + r*rb) is
+// RN(a/b) when nothing underflows.  When q is zero, infinite or NaN (zero,
+// infinite or NaN numerator; zero or infinite divisor) q itself has the IEEE
+// quotient's value and sign and is returned.  Three FP64 operations instead
+// of a full division where one divisor serves several quotients.
+SPD_FN double div_rcp(double a, double b, double rb) {
+  const double q = a * rb;
+  const double r = fma(-q, b, a);
+  const double q2 = fma(r, rb, q);
+#ifdef __CUDA_ARCH__
+  const long long bits = __double_as_longlong(q) & 0x7fffffffffffffffLL;
+#else
+  long long bits;
+  memcpy(&bits, &q, sizeof(bits));
+  bits &= 0x7fffffffffffffffLL;
+#endif
+  return (bits == 0 || bits >= 0x7ff0000000000000LL) ? q : q2;
+}
+
 SPD_FN double sval(double x) { return x; }
 template <int N> SPD_FN double sval(const Dual<N>& x) { return x.v; }
 SPD_FN double ad_sqrt(double x) { return sqrt(x); }
@@ -117,6 +141,17 @@ SPD_FN Dual<N> ad_abs(const Dual<N>& x) {
   if (x.v < 0) return -x;
   return Dual<N>(fabs(x.v));
 }
+
+// a / b with b's reciprocal rb precomputed (double: Markstein; dual numbers:
+// plain division, rb unused)
+SPD_FN double div_by(double a, double b, double rb) { return div_rcp(a, b, rb); }
+template <int N>
+SPD_FN Dual<N> div_by(const Dual<N>& a, const Dual<N>& b, const Dual<N>&) { return a / b; }
+template <int N>
+SPD_FN Dual<N> div_by(const Dual<N>& a, double b, double) { return a / b; }
+SPD_FN double recip_of(double b) { return 1.0 / b; }
+template <int N>
+SPD_FN Dual<N> recip_of(const Dual<N>&) { return Dual<N>(0.0); }
 
 // NumPy's maximum / minimum: NaN in either argument propagates.
 template <class S>
@@ -188,10 +223,11 @@ SPD_FN void prim(const S* U, S* W, double gamma, int idim_order) {
   constexpr int P_ = D + 1;
   W[0] = U[0];
   S K = 0.0;
+  const S r0 = recip_of(U[0]);
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const int v = rvel<D>(idim_order, k);
-    W[v] = U[v] / U[0];
+    W[v] = (D == 1) ? U[v] / U[0] : div_by(U[v], U[0], r0);
     const S w2 = W[v] * W[v];
     K = (k == 0) ? w2 : K + w2;
   }
@@ -213,7 +249,7 @@ SPD_FN void cons(const S* W, S* U, double gamma, int idim_order) {
     K = (k == 0) ? w2 : K + w2;
   }
   K = K * (0.5 * W[0]);
-  U[P_] = W[P_] / (gamma - 1.0) + K;
+  U[P_] = div_by(W[P_], gamma - 1.0, 1.0 / (gamma - 1.0)) + K;
 }
 
 // Euler flux in the rotated frame of direction idim (src/hydro.py:127-170).
@@ -230,7 +266,7 @@ SPD_FN void flux(const S* W, S* F, double gamma, int idim) {
     K = (k == D - 1) ? mv : K + mv;
     F[v] = m * W[v1];
   }
-  const S E = W[P_] / (gamma - 1.0) + 0.5 * K;
+  const S E = div_by(W[P_], gamma - 1.0, 1.0 / (gamma - 1.0)) + 0.5 * K;
   F[0] = m;
   F[v1] = m * W[v1] + W[P_];
   F[P_] = W[v1] * (E + W[P_]);
@@ -278,7 +314,8 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
   const S rcL = WL[0] * (vL - sL);
   const S rcR = WR[0] * (sR - vR);
   const S den = rcR + rcL;
-  const S vstar = (rcR * vR + rcL * vL + (WL[P_] - WR[P_])) / den;
+  const S rden = recip_of(den);
+  const S vstar = div_by(rcR * vR + rcL * vL + (WL[P_] - WR[P_]), den, rden);
   S Pstar;
   if (low_mach) {
     S mx, Mach;
@@ -291,22 +328,24 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
       Mach = pick(br, S(1.0) <= mx) ? S(1.0) : mx;
     }
     const S phi = Mach * (2.0 - Mach);
-    Pstar = (rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR)) / den;
+    Pstar = div_by(rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR), den, rden);
   } else {
-    Pstar = (rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR)) / den;
+    Pstar = div_by(rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR), den, rden);
   }
   S r, vg, Pg, e;
   if (pick(br, sL > 0.0)) {
     r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
   } else if (pick(br, vstar > 0.0)) {
     const S d = sL - vstar;
-    r = WL[0] * (sL - vL) / d;
-    e = ((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar) / d;
+    const S rd = recip_of(d);
+    r = div_by(WL[0] * (sL - vL), d, rd);
+    e = div_by((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar, d, rd);
     vg = vstar; Pg = Pstar;
   } else if (pick(br, sR > 0.0)) {
     const S d = sR - vstar;
-    r = WR[0] * (sR - vR) / d;
-    e = ((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar) / d;
+    const S rd = recip_of(d);
+    r = div_by(WR[0] * (sR - vR), d, rd);
+    e = div_by((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar, d, rd);
     vg = vstar; Pg = Pstar;
   } else {
     r = WR[0]; vg = vR; Pg = WR[P_]; e = UR[P_];

@@ -13,6 +13,8 @@ struct FvGeo {
   const double* centers[3];  // extended subcell centres, Xe_d values
   const double* hfp[3];      // extended subcell widths, Xe_d values
   const double* hcv[3];      // extended centre distances, Xe_d - 1 values
+  const double* rdx[3];      // 1 / dx (correctly rounded)
+  const double* rhcv[3];     // 1 / hcv (correctly rounded)
 };
 
 __device__ __forceinline__ void q_coords(const Geo& g, long long q, int& ix, int& iy, int& iz) {
@@ -52,7 +54,8 @@ __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, i
     const long long nf = n_faces(g, d);
     const long long fl = face_id(g, d, ix, iy, iz);
     const long long fr = face_id(g, d, ix + (d == 0), iy + (d == 1), iz + (d == 2));
-    const double part = (F[d][(long long)v * nf + fr] - F[d][(long long)v * nf + fl]) / fg.dx[d][ii[d]];
+    const double part = div_rcp(F[d][(long long)v * nf + fr] - F[d][(long long)v * nf + fl], fg.dx[d][ii[d]],
+                                fg.rdx[d][ii[d]]);
     acc = (d == 0) ? part : acc + part;
   }
   out = acc;
@@ -455,11 +458,12 @@ __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __rest
     const long long st = ext_stride(g, d);
     const int k = c[d];
     const double hl = fg.hcv[d][k - 1], hr = fg.hcv[d][k], hm = fg.hfp[d][k];
+    const double rhl = fg.rhcv[d][k - 1], rhr = fg.rhcv[d][k];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       const double* M = W_ext + (long long)v * g.Nqe;
-      const double SL = (M[e] - M[e - st]) / hl;
-      const double SR = (M[e + st] - M[e]) / hr;
+      const double SL = div_rcp(M[e] - M[e - st], hl, rhl);
+      const double SR = div_rcp(M[e + st] - M[e], hr, rhr);
       double dm;
       if (BM == 0) dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
       else dm = limiter_br<BM>(limiter, SL, SR, hl, hr, hm, &ltape[((long long)d * V + v) * g.Nqe + e]);
@@ -560,7 +564,7 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
         else if (a != 0.0) Fv[s] = a * FB[d][(long long)v * nf + fs[s]] + (1.0 - a) * ho;
         else Fv[s] = ho;
       }
-      const double part = (Fv[1] - Fv[0]) / fg.dx[d][ii[d]];
+      const double part = div_rcp(Fv[1] - Fv[0], fg.dx[d][ii[d]], fg.rdx[d][ii[d]]);
       acc = (d == 0) ? part : acc + part;
     }
     U_new[(long long)v * g.Nq + q] = U_cv[(long long)v * g.Nq + q] - acc * dti;

@@ -280,7 +280,7 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
 #pragma unroll
             for (int so = 0; so < k::n; ++so) {
               const double dsum = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d);
-              const double val = pow2 ? dsum * ihd : dsum / hd;
+              const double val = pow2 ? dsum * ihd : div_rcp(dsum, hd, ihd);
               const int s = sp_index<D, P>(d, j, so);
               double* slot = &dudt_s[(((long long)v * k::NS + s) * Teff + tl) * CPB + cl];
               *slot = (d == 0) ? val : *slot + val;

@@ -2,10 +2,14 @@
 // pointwise Euler maps (spd_vjp.cuh) against products formed with the
 // dual-number forms of the same maps (spd_device.cuh): random states in 1D,
 // 2D and 3D, every Riemann solver, conservative and primitive inputs, and
-// mirrored states (the velocity ties of reflective walls).  Exit status 0
-// when every relative difference is below 1e-12.
+// mirrored states (the velocity ties of reflective walls); and the
+// Markstein quotient div_rcp against IEEE division, bit for bit.  Exit
+// status 0 when every relative difference is below 1e-12 and no quotient
+// differs.
 #include <cstdio>
+#include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <random>
 #include "spd_vjp.cuh"
 using namespace spd;
@@ -80,9 +84,33 @@ double check_flux_prim(std::mt19937_64& rng, int d) {
   return sqrt(err / nrm);
 }
 
+// div_rcp (Markstein's correction from a correctly rounded reciprocal)
+// against the correctly rounded IEEE quotient: returns the mismatch count.
+long long check_div_rcp(std::mt19937_64& rng, long long n) {
+  std::uniform_int_distribution<int> ea(-80, 80), eb(-40, 40);
+  std::uniform_real_distribution<double> m(1.0, 2.0);
+  long long bad = 0;
+  const double specials[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, 1.0, -1.0, 0.4, 3.0};
+  for (long long i = 0; i < n; ++i) {
+    double a = std::ldexp(m(rng), ea(rng)) * ((rng() & 1) ? -1.0 : 1.0);
+    double b = std::ldexp(m(rng), eb(rng)) * ((rng() & 1) ? -1.0 : 1.0);
+    if (i % 97 == 0) a = specials[(i / 97) % 9];
+    if (i % 89 == 0) b = specials[5 + (i / 89) % 4];
+    if (i % 7 == 0) b = 0.4;  // gamma - 1
+    volatile double rb = 1.0 / b;
+    const double got = div_rcp(a, b, rb);
+    const double want = a / b;
+    if (!(std::memcmp(&got, &want, sizeof(double)) == 0 || (got != got && want != want))) ++bad;
+  }
+  return bad;
+}
+
 int main() {
   std::mt19937_64 rng(42);
   double worst = 0.0;
+  const long long div_bad = check_div_rcp(rng, 20000000);
+  printf("div_rcp mismatches: %lld of 20000000\n", div_bad);
+  if (div_bad) return 1;
   for (int trial = 0; trial < 4000; ++trial) {
     for (int solver = 0; solver < 3; ++solver)
       for (int prims = 0; prims < 2; ++prims) {
