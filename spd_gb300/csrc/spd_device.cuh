@@ -134,7 +134,15 @@ SPD_FN Dual<N> ad_sqrt(const Dual<N>& x) {
   for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
   return r;
 }
-SPD_FN double ad_abs(double x) { return fabs(x); }
+// |x| by clearing the sign bit (integer pipe; the same bits as fabs)
+SPD_FN double abs_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+#else
+  return fabs(x);
+#endif
+}
+SPD_FN double ad_abs(double x) { return abs_bits(x); }
 template <int N>
 SPD_FN Dual<N> ad_abs(const Dual<N>& x) {
   if (x.v > 0) return x;
@@ -158,6 +166,26 @@ template <class S>
 SPD_FN S np_max(const S& a, const S& b) { return (a >= b || a != a) ? a : b; }
 template <class S>
 SPD_FN S np_min(const S& a, const S& b) { return (a <= b || a != a) ? a : b; }
+// The same two functions for doubles on the device, evaluated on integer
+// keys that order the doubles as IEEE comparison does (-0 equal to +0,
+// NaN first): identical results, no FP64-pipe comparison.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ long long ieee_key(long long b) {
+  b = (b == (long long)0x8000000000000000ULL) ? 0 : b;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+template <>
+__device__ __forceinline__ double np_max<double>(const double& a, const double& b) {
+  const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+  return (nan_bits(ba) || (!nan_bits(bb) && ieee_key(ba) >= ieee_key(bb))) ? a : b;
+}
+template <>
+__device__ __forceinline__ double np_min<double>(const double& a, const double& b) {
+  const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+  return (nan_bits(ba) || (!nan_bits(bb) && ieee_key(ba) <= ieee_key(bb))) ? a : b;
+}
+#endif
 // Dual forms: same value; at a tie the derivative is the mean of the two
 // arguments' derivatives (the subgradient torch.maximum / torch.minimum
 // propagate).
@@ -424,8 +452,8 @@ SPD_FN double np_sign(double x) {
 }
 SPD_FN double moncen(double dUL, double dUR, double dxL, double dxR, double dxM) {
   const double dUC = (dxL * dUL + dxR * dUR) / (dxL + dxR);
-  double slope = np_min(fabs(2.0 * dUL * dxL / dxM), fabs(2.0 * dUR * dxR / dxM));
-  slope = np_sign(dUC) * np_min(slope, fabs(dUC));
+  double slope = np_min(abs_bits(2.0 * dUL * dxL / dxM), abs_bits(2.0 * dUR * dxR / dxM));
+  slope = np_sign(dUC) * np_min(slope, abs_bits(dUC));
   return (dUL * dUR >= 0.0) ? slope : 0.0;
 }
 

@@ -43,6 +43,21 @@ __host__ __device__ __forceinline__ long long n_faces(const Geo& g, int d) {
   return (long long)(g.X[0] + (d == 0)) * (g.X[1] + (d == 1)) * (g.X[2] + (d == 2));
 }
 
+// Order-preserving int64 key of a double (ordering of the non-NaN values,
+// -0 mapped to +0 so that the two zeros compare equal as in IEEE) and its
+// inverse; NaN test on the bits.
+__device__ __forceinline__ long long order_key(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double from_order_key(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
 // dUdt of one subcell from the face fluxes (src/fv_simulator.py:189-205)
 template <int D>
 __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, int ix, int iy, int iz,
@@ -164,27 +179,34 @@ __global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __r
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       const double* W = ext_old + (long long)v * g.Nqe;
+      // maximum / minimum of the cross stencil on order-preserving integer
+      // keys (integer pipes; the FP64 pipe is the step's bottleneck).  A NaN
+      // anywhere makes NumPy's maximum/minimum NaN and the point troubled.
       const double c0 = W[e];
-      double mx = c0, mn = c0;
+      bool nan = is_nan_bits(c0);
+      long long kmx = order_key(c0), kmn = kmx;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const long long st = ext_stride(g, d);
         const double a = W[e - st], b = W[e + st];
-        mx = np_max(np_max(a, b), mx);
-        mn = np_min(np_min(a, b), mn);
+        nan = nan || is_nan_bits(a) || is_nan_bits(b);
+        const long long ka = order_key(a), kb = order_key(b);
+        kmx = max(kmx, max(ka, kb));
+        kmn = min(kmn, min(ka, kb));
       }
+      double mx = from_order_key(kmx), mn = from_order_key(kmn);
       if (relax) {
         if (delta) {
           const double eps = tol * (mx - mn);
           mn = mn - eps;
           mx = mx + eps;
         } else {
-          mn = mn - fabs(mn) * tol;
-          mx = mx + fabs(mx) * tol;
+          mn = mn - abs_bits(mn) * tol;
+          mx = mx + abs_bits(mx) * tol;
         }
       }
       const double wn = ext_new[(long long)v * g.Nqe + e];
-      const bool pt = !(wn >= mn) || !(wn <= mx);
+      const bool pt = nan || !(wn >= mn) || !(wn <= mx);
       m |= (pt ? 1u : 0u) << v;
     }
     mask[q] = (unsigned char)m;
@@ -590,7 +612,7 @@ __global__ void k_wcv_cmax(Geo g, const double* __restrict__ U_cv, double* __res
     for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
     double c = sound_speed(W[P_], W[0], g.gamma, g.min_c2) * (double)D;
 #pragma unroll
-    for (int v = 1; v <= D; ++v) c = c + fabs(W[v]);
+    for (int v = 1; v <= D; ++v) c = c + abs_bits(W[v]);
     if (c != c) isnan_c = true;
     else cval = c;
   }

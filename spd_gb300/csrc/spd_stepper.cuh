@@ -17,7 +17,7 @@ __global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned lon
   if (q < g.Nq) {
     double c = sound_speed(W_cv[(long long)P_ * g.Nq + q], W_cv[q], g.gamma, g.min_c2) * (double)D;
 #pragma unroll
-    for (int v = 1; v <= D; ++v) c = c + fabs(W_cv[(long long)v * g.Nq + q]);
+    for (int v = 1; v <= D; ++v) c = c + abs_bits(W_cv[(long long)v * g.Nq + q]);
     if (c != c) isnan_c = true;
     else cval = c;
   }
