@@ -197,7 +197,7 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   // subcell geometry (src/sdader_simulator.py:61-92, src/fv_simulator.py:195)
   {
     std::vector<double> buf;
-    size_t off[3][6];
+    size_t off[3][8];
     for (int d = 0; d < D; ++d) {
       const int Xd = g.X[d], Xe = g.Xe[d];
       const double* fp = ops->faces[d];
@@ -215,6 +215,10 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
       for (int k2 = 0; k2 < Xd; ++k2) buf.push_back(1.0 / buf[off[d][0] + k2]);
       off[d][5] = buf.size();
       for (int e = 0; e + 1 < Xe; ++e) buf.push_back(1.0 / buf[off[d][3] + e]);
+      off[d][6] = buf.size();
+      for (int e = 0; e < Xe; ++e) buf.push_back((e >= 1 && e + 1 < Xe) ? cen[e + 1] - cen[e - 1] : 1.0);
+      off[d][7] = buf.size();
+      for (int e = 0; e < Xe; ++e) buf.push_back(1.0 / buf[off[d][6] + e]);
     }
     if (int r = dalloc(C, &C->geo_arrays, buf.size())) return r;
     CK(cudaMemcpy(C->geo_arrays, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -225,6 +229,8 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
       C->fvg.hcv[d] = C->geo_arrays + off[d][3];
       C->fvg.rdx[d] = C->geo_arrays + off[d][4];
       C->fvg.rhcv[d] = C->geo_arrays + off[d][5];
+      C->fvg.c2[d] = C->geo_arrays + off[d][6];
+      C->fvg.rc2[d] = C->geo_arrays + off[d][7];
     }
   }
   // state and scratch

@@ -246,16 +246,18 @@ SPD_FN int rvel(int idim, int k) { return 1 + (idim + k) % D; }
 // U -> W (src/hydro.py:48-86); the kinetic term sums in the order of the
 // velocity list, which is the rotated list inside the Riemann wrapper
 // (src/riemann_solver.py:10-29) and the plain list elsewhere.
+// ``r0_out`` (optional) receives 1/rho for later quotients by rho.
 template <int D, class S>
-SPD_FN void prim(const S* U, S* W, double gamma, int idim_order) {
+SPD_FN void prim(const S* U, S* W, double gamma, int idim_order, S* r0_out = nullptr) {
   constexpr int P_ = D + 1;
   W[0] = U[0];
   S K = 0.0;
   const S r0 = recip_of(U[0]);
+  if (r0_out) *r0_out = r0;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const int v = rvel<D>(idim_order, k);
-    W[v] = (D == 1) ? U[v] / U[0] : div_by(U[v], U[0], r0);
+    W[v] = (D == 1 && !r0_out) ? U[v] / U[0] : div_by(U[v], U[0], r0);
     const S w2 = W[v] * W[v];
     K = (k == 0) ? w2 : K + w2;
   }
@@ -303,8 +305,8 @@ SPD_FN void flux(const S* W, S* F, double gamma, int idim) {
 // Sound speed with floor (src/hydro.py:3-46).
 template <class S, int BM = 0>
 SPD_FN S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
-                                         Br<BM>* br = nullptr) {
-  S c2 = gamma * P / rho;
+                                         Br<BM>* br = nullptr, const S* rrho = nullptr) {
+  S c2 = rrho ? div_by(gamma * P, rho, *rrho) : gamma * P / rho;
   c2 = pick(br, c2 > min_c2) ? c2 : S(min_c2);
   return ad_sqrt(c2);
 }
@@ -312,14 +314,15 @@ SPD_FN S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
 // LLF (src/riemann_solver.py:31-65).
 template <int D, class S, int BM = 0>
 SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
-                                    double min_c2, int idim, Br<BM>* br = nullptr) {
+                                    double min_c2, int idim, Br<BM>* br = nullptr, const S* rL = nullptr,
+                                    const S* rR = nullptr) {
   constexpr int V = D + 2, P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
   S FL[V], FR[V];
   flux<D>(WL, FL, gamma, idim);
   flux<D>(WR, FR, gamma, idim);
-  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br) + abs_br(WL[v1], br);
-  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br) + abs_br(WR[v1], br);
+  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
+  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br, rR) + abs_br(WR[v1], br);
   const S cmax = pick(br, cL > cR) ? cL : cR;
   const S hc = 0.5 * cmax;
 #pragma unroll
@@ -330,11 +333,12 @@ SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double
 // Only the branch the reference's np.where chain selects is evaluated.
 template <int D, class S, int BM = 0>
 SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
-                                     double min_c2, int idim, bool low_mach, Br<BM>* br = nullptr) {
+                                     double min_c2, int idim, bool low_mach, Br<BM>* br = nullptr,
+                                     const S* rL = nullptr, const S* rR = nullptr) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
-  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br) + abs_br(WL[v1], br);
-  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br) + abs_br(WR[v1], br);
+  const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
+  const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br, rR) + abs_br(WR[v1], br);
   const S cmax = pick(br, cL > cR) ? cL : cR;
   const S vL = WL[v1], vR = WR[v1];
   const S sL = (pick(br, vL < vR) ? vL : vR) - cmax;
@@ -398,6 +402,9 @@ SPD_FN void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, do
                                         int idim, bool prims, Br<BM>* br = nullptr) {
   constexpr int V = D + 2;
   S WL[V], WR[V], UL[V], UR[V];
+  S rL, rR;  // 1/rho of the two states when the conversion computed it
+  const S* prL = nullptr;
+  const S* prR = nullptr;
   if (prims) {
 #pragma unroll
     for (int v = 0; v < V; ++v) { WL[v] = ML[v]; WR[v] = MR[v]; }
@@ -406,11 +413,13 @@ SPD_FN void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, do
   } else {
 #pragma unroll
     for (int v = 0; v < V; ++v) { UL[v] = ML[v]; UR[v] = MR[v]; }
-    prim<D>(UL, WL, gamma, idim);
-    prim<D>(UR, WR, gamma, idim);
+    prim<D>(UL, WL, gamma, idim, &rL);
+    prim<D>(UR, WR, gamma, idim, &rR);
+    prL = &rL;
+    prR = &rR;
   }
-  if (solver == RS_LLF) llf<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, br);
-  else hllc<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC, br);
+  if (solver == RS_LLF) llf<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, br, prL, prR);
+  else hllc<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC, br, prL, prR);
 }
 
 // One output of a 1D operator contraction: sum_s A[s] * x[s].  ``lanes2``

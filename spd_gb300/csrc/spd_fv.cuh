@@ -15,6 +15,8 @@ struct FvGeo {
   const double* hcv[3];      // extended centre distances, Xe_d - 1 values
   const double* rdx[3];      // 1 / dx (correctly rounded)
   const double* rhcv[3];     // 1 / hcv (correctly rounded)
+  const double* c2[3];       // centres[j+1] - centres[j-1], Xe_d values (ends unused)
+  const double* rc2[3];      // 1 / c2 (correctly rounded)
 };
 
 __device__ __forceinline__ void q_coords(const Geo& g, long long q, int& ix, int& iy, int& iz) {
@@ -219,31 +221,42 @@ __global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __r
 // active subcell i (src/trouble_detection.py:104-137, including its
 // one-sided minimum at the first and last active subcell).
 __device__ __forceinline__ double sed_alpha_dir(const double* W, long long e0, long long st, int i, int Xd,
-                                                const double* cen, const double* hfp) {
-  // line accessors in extended coordinates k along d
-  auto U = [&](int k) { return W[e0 + (long long)k * st]; };
-  auto dU = [&](int k) { return (U(k + 1) - U(k - 1)) / (cen[k + 1] - cen[k - 1]); };
-  auto aLR = [&](int k, double& aL, double& aR) {
-    const double dUm = dU(k - 1), dU0 = dU(k), dUp = dU(k + 1);
-    const double d2U = (dUp - dUm) / (cen[k + 1] - cen[k - 1]);
-    const double dv = 0.5 * hfp[k] * d2U;
+                                                const double* c2, const double* rc2, const double* hfp) {
+  // line accessors in extended coordinates j along d; c2[j] = cen[j+1] -
+  // cen[j-1] and rc2[j] its correctly rounded reciprocal (the quotients
+  // below are the IEEE ones, div_rcp)
+  auto U = [&](int j) { return W[e0 + (long long)j * st]; };
+  const int k = i + NGH;
+  const int lo = (i == 0) ? k - 1 : k - 2;
+  const int hi = (i == Xd - 1) ? k + 1 : k + 2;
+  double dUs[5];
+#pragma unroll
+  for (int o = 0; o < 5; ++o) {
+    const int j = k - 2 + o;
+    if (j >= lo && j <= hi) dUs[o] = div_rcp(U(j + 1) - U(j - 1), c2[j], rc2[j]);
+  }
+  auto dU = [&](int j) { return dUs[j - (k - 2)]; };
+  auto aLR = [&](int kk, double& aL, double& aR) {
+    const double dUm = dU(kk - 1), dU0 = dU(kk), dUp = dU(kk + 1);
+    const double d2U = div_rcp(dUp - dUm, c2[kk], rc2[kk]);
+    const double dv = 0.5 * hfp[kk] * d2U;
+    const double rdv = 1.0 / dv;
     const double vL = dUm - dU0;
     const double vR = dUp - dU0;
     const double selL = (dv < 0) ? ((vL > 0) ? vL : 0.0) : ((vL < 0) ? vL : 0.0);
-    aL = -selL / dv;
-    if (fabs(dv) <= 0.0) aL = 1.0;
+    aL = div_rcp(-selL, dv, rdv);
+    if (abs_bits(dv) <= 0.0) aL = 1.0;
     aL = (aL < 1.0) ? aL : 1.0;
     const double selR = (dv > 0) ? ((vR > 0) ? vR : 0.0) : ((vR < 0) ? vR : 0.0);
-    aR = selR / dv;
-    if (fabs(dv) <= 0.0) aR = 1.0;
+    aR = div_rcp(selR, dv, rdv);
+    if (abs_bits(dv) <= 0.0) aR = 1.0;
     aR = (aR < 1.0) ? aR : 1.0;
   };
-  auto A = [&](int k) {
+  auto A = [&](int kk) {
     double aL, aR;
-    aLR(k, aL, aR);
+    aLR(kk, aL, aR);
     return (aR < aL) ? aR : aL;
   };
-  const int k = i + NGH;
   if (i == 0) return np_min(A(k), A(k + 1));
   if (i == Xd - 1) {
     double aL, aR;
@@ -280,7 +293,7 @@ __global__ void k_troubles(Geo g, FvGeo fg, int sed_enabled, int pad, double min
       for (int d = 0; d < D; ++d) {
         const long long st = ext_stride(g, d);
         const long long e0 = e - (long long)(ii[d] + NGH) * st;
-        const double an = sed_alpha_dir(W, e0, st, ii[d], g.X[d], fg.centers[d], fg.hfp[d]);
+        const double an = sed_alpha_dir(W, e0, st, ii[d], g.X[d], fg.c2[d], fg.rc2[d], fg.hfp[d]);
         alpha = (an < alpha) ? an : alpha;
       }
       *pts[w] = (alpha < 1.0) ? *pts[w] : 0;
