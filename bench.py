@@ -325,8 +325,13 @@ def ours(args):
         per_launch_bytes = bytes_step / nlaunch_per_step
         avg_s = top[1][1] / top[1][0] / 1e3
         achieved = per_launch_bytes / avg_s / 1e9
+        # DRAM bytes (read + write) per k_interior launch from one ncu capture of
+        # the 2D p=3 four-quadrant step at 256^2 (mean over the 4 launches of a
+        # step: 338, 473, 474, 594 MB; profiles/k_interior_quadrant256_p3.md),
+        # scaled by the cell count (traffic grows in proportion)
+        traffic = 469.811968e6 * cells / 65536 if (D, p) == (2, 3) else None
         roof = {"bound": "hbm", "kernel": "k_interior", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved / peak_gbs, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak_gbs, "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3}
     fp64 = None
     if rank == 0:
