@@ -35,6 +35,11 @@ WORKLOADS = {
                    "MUSCL-Hancock fallback, HLLC, transmissive boundaries",
     "vortex32": "isentropic vortex, 32x32 cells, p=3, FV update with limiting, LLF, periodic",
     "sedov128": "3D Sedov blast, 128^3 cells, p=2, FV update with limiting, HLLC, reflective",
+    "vortex512_sd": "isentropic vortex on [0,10]^2, 512x512 cells, p=3, SD update (no limiter), LLF, periodic",
+    "quadrant512_lhllc_moncen": "four-quadrant Riemann problem, 512x512 cells, p=3, FV update with limiting, "
+                                "low-Mach HLLC, moncen slopes, transmissive boundaries",
+    "kh_ensemble_small": "batched: 256 periodic Kelvin-Helmholtz shear layers, p=3, sides drawn from "
+                         "{16,24,32,48,64} (seed 2026), HLLC + limiting, per-instance dt",
     "kh_ensemble": "batched: 64 periodic Kelvin-Helmholtz shear layers, p=3, sides drawn from "
                    "{64,128,192,256,384,512} (seed 2026), HLLC + limiting, per-instance dt",
     "kh_adjoint": "gradient of J = ||rho(T) - rho_target||^2 with respect to the initial density, periodic "
@@ -54,6 +59,15 @@ def workload_kwargs(name, n_override=None):
         n = n_override or 32
         return dict(p=3, N=(n, n), xlim=(0, 10), ylim=(0, 10), init_fct=ics.isentropic_vortex(), update="FV",
                     FB=True, riemann_solver_sd="llf", riemann_solver_fv="llf", BC=(("periodic", "periodic"),) * 2)
+    if name == "vortex512_sd":
+        n = n_override or 512
+        return dict(p=3, N=(n, n), xlim=(0, 10), ylim=(0, 10), init_fct=ics.isentropic_vortex(), update="SD",
+                    riemann_solver_sd="llf", BC=(("periodic", "periodic"),) * 2)
+    if name == "quadrant512_lhllc_moncen":
+        n = n_override or 512
+        return dict(p=3, N=(n, n), init_fct=ics.four_quadrant, update="FV", FB=True, riemann_solver_sd="lhllc",
+                    riemann_solver_fv="lhllc", slope_limiter="moncen", BC=(("gradfree", "gradfree"),) * 2,
+                    cfl_coeff=0.8)
     if name == "sedov128":
         n = n_override or 128
         return dict(p=2, N=(n, n, n), init_fct=ics.sedov(n), update="FV", FB=True, riemann_solver_sd="hllc",
@@ -194,8 +208,9 @@ def _cpu_worker(args):
         state[f"BC_fv_{d}"] = np.zeros((2, ndim + 2) + tuple(ext[::-1]))
     o = OracleSDADER(ndim=ndim, N=list(kw["N"]), p=p, m=p, lims=lims, BC=kw["BC"], gamma=1.4,
                      cfl_coeff=kw.get("cfl_coeff", 0.8), min_c2=1e-10, riemann_solver_sd=kw["riemann_solver_sd"],
-                     riemann_solver_fv=kw["riemann_solver_fv"], slope_limiter="minmod", update=kw["update"],
-                     FB=kw["FB"], tolerance=1e-5, SED=True, NAD="", PAD=True, blending=True, min_rho=1e-10,
+                     riemann_solver_fv=kw.get("riemann_solver_fv", "llf"),
+                     slope_limiter=kw.get("slope_limiter", "minmod"), update=kw["update"],
+                     FB=kw.get("FB", False), tolerance=1e-5, SED=True, NAD="", PAD=True, blending=True, min_rho=1e-10,
                      max_rho=1e10, min_P=1e-10, godunov=False, ops=ops, state=state)
     for _ in range(warmup):
         o.compute_dt()
@@ -224,7 +239,8 @@ def reference_arm(args):
     if rank != 0:
         return
     procs = os.cpu_count() or 1
-    n_side = {"quadrant512": 64, "vortex32": 32, "sedov128": 12}[args.workload]
+    n_side = {"quadrant512": 64, "vortex32": 32, "sedov128": 12, "vortex512_sd": 64,
+              "quadrant512_lhllc_moncen": 64}[args.workload]
     steps = max(1, args.steps)
     value, tmax = cpu_baseline(args.workload, n_side, steps, args.warmup, procs)
     kw = workload_kwargs(args.workload, n_side)
@@ -343,9 +359,10 @@ def ours(args):
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            v, tmax = cpu_baseline(args.workload, 128, 1, 0, 1)
+            sample_n = 128 if len(kw["N"]) == 2 else 16
+            v, tmax = cpu_baseline(args.workload, sample_n, 1, 0, 1)
             cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                   "sample": "1 step of the same configuration at 128x128 cells on one core "
+                   "sample": f"1 step of the same configuration at {'x'.join([str(sample_n)] * len(kw['N']))} cells on one core "
                              "(CPU restatement of the reference's NumPy path)"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -374,7 +391,9 @@ def ensemble_arm(args):
     from spd_gb300 import SDADER_Ensemble, SDADER_Simulator
     from spd_gb300.initial_conditions import kelvin_helmholtz
     rng = np.random.default_rng(2026)
-    sides = [int(x) for x in rng.choice([64, 128, 192, 256, 384, 512], size=args.instances)]
+    small = args.workload == "kh_ensemble_small"
+    choices = [16, 24, 32, 48, 64] if small else [64, 128, 192, 256, 384, 512]
+    sides = [int(x) for x in rng.choice(choices, size=args.instances)]
 
     def make(i, n):
         return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=1000 + i), update="FV", FB=True,
@@ -408,7 +427,7 @@ def ensemble_arm(args):
     line = {"metric": METRIC + "; batched/plain speedup", "value": batched, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_s / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS["kh_ensemble"], "instances": len(sides), "sides": sides,
+            "config": {"workload": WORKLOADS[args.workload], "instances": len(sides), "sides": sides,
                        "dof_per_ensemble_step": dof},
             "plain_loop_value": plain, "batched_over_plain": batched / plain, "autotune": tuning}
     print(json.dumps(line), flush=True)
@@ -607,9 +626,11 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
-    elif args.workload == "kh_ensemble":
+    elif args.workload in ("kh_ensemble", "kh_ensemble_small"):
         from spd_gb300.build import build
         build()
+        if args.workload == "kh_ensemble_small" and args.instances == 64:
+            args.instances = 256
         ensemble_arm(args)
     elif args.workload == "kh_adjoint":
         from spd_gb300.build import build

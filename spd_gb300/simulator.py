@@ -583,6 +583,48 @@ class SDADER_Simulator:
             print(f"dt={self.dm.dt}")
         self.end_sim()
 
+    # ------------------------------------------------------------------
+    # state snapshots (no counterpart in the reference, which has no
+    # save/load): the device state, time, step count and dt in one .npz
+    # ------------------------------------------------------------------
+    def _snapshot_config(self) -> dict:
+        return dict(ndim=self.ndim, N=[self.N[d] for d in self.dims], p=self.p, m=self.m, update=self.update,
+                    FB=bool(self.FB), riemann_solver_sd=self.riemann_solver_sd_name,
+                    riemann_solver_fv=self.riemann_solver_fv_name, slope_limiter=self.slope_limiter_name,
+                    BC=[list(self.BC[d]) for d in self.dims], gamma=self.gamma, cfl_coeff=self.cfl_coeff,
+                    lims=[list(self.lim[d]) for d in self.dims])
+
+    def save_state(self, path) -> None:
+        """Write U_sp, U_cv, W_cv, the FV boundary buffers, time, n_step, dt
+        and the configuration to ``path`` (.npz)."""
+        import json
+        arrays = {name: self._download(name) for name in ("U_sp", "U_cv", "W_cv")}
+        if self.update == "FV":
+            for d in self.dims:
+                idim = self.dims[d]
+                ext = [self.N[DIMS[i]] * (self.p + 1) + 2 * self.Nghc for i in range(self.ndim)]
+                ext[idim] = self.Nghc
+                arrays[f"BC_fv_{d}"] = self._ctx.download(f"BC_fv_{d}", (2, self.nvar) + tuple(ext[::-1]))
+        np.savez(path, time=np.float64(self.time), n_step=np.int64(self.n_step), dt=np.float64(self._ctx.get_dt()),
+                 config=json.dumps(self._snapshot_config()), **arrays)
+
+    def restore_state(self, path) -> None:
+        """Load a snapshot written by ``save_state`` of a simulator built with
+        the same configuration; the run then continues bit for bit."""
+        import json
+        z = np.load(path)
+        cfg = json.loads(str(z["config"]))
+        if cfg != json.loads(json.dumps(self._snapshot_config())):
+            raise ValueError(f"snapshot configuration differs: {cfg}")
+        for name in ("U_sp", "U_cv", "W_cv"):
+            self._ctx.upload(name, z[name])
+        if self.update == "FV":
+            for d in self.dims:
+                self._ctx.upload(f"BC_fv_{d}", z[f"BC_fv_{d}"])
+        self.time = float(z["time"])
+        self.n_step = int(z["n_step"])
+        self._ctx.set_dt(float(z["dt"]))
+
     def close(self):
         if self._ctx is not None:
             self._ctx.close()
