@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-rdc=false",
          "-Wno-deprecated-gpu-targets"]
 SOURCES = ["spd_core.cu", "spd_step_d1.cu", "spd_step_d2.cu", "spd_step_d3.cu", "spd_noalloc.cu", "spd_ensemble.cu",
-           "spd_adjoint.cu"]
+           "spd_adjoint.cu", "spd_adj_d1.cu", "spd_adj_d2.cu", "spd_adj_d3.cu"]
+
 
 
 def nvcc() -> str:

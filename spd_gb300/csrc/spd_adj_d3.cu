@@ -1,0 +1,4 @@
+// Adjoint launch sequences for 3D (p = 1..4).
+#include "spd_adjoint_exec.cuh"
+
+SPD_INSTANTIATE_ADJOINT(3)

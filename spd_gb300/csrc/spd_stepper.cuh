@@ -2,10 +2,12 @@
 // (src/sdader_simulator.py:361-378); instantiated per dimension in
 // spd_step_d1.cu, spd_step_d2.cu and spd_step_d3.cu.
 #pragma once
-#include "spd_adjoint.cuh"
 #include "spd_ctx.cuh"
 
 namespace spd_host {
+
+template <int D, int P>
+int adjoint_vjp(spd_ctx* C);
 
 template <int D, int P>
 __global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned long long* __restrict__ cmax_bits,
@@ -372,185 +374,9 @@ struct Stepper : StepperBase {
     return 0;
   }
 
-  // ---- adjoint ----------------------------------------------------------
-  int traces_of(spd_ctx* C, const double* U, int Tu, int Teff) {
-    const Geo& g = C->geo;
-    ProfScope ps_(C, "k_adj_traces_fwd");
-    k_traces_ader<D, P><<<blocks_for(g.Nc * Teff, 128), 128, 0, C->stream>>>(C->ops, g, U, Tu, Teff, C->trace[0],
-                                                                            C->trace[1], C->trace[2]);
-    CKL();
-    return 0;
-  }
-
-  // adjoint of one predictor iteration: dudt_a (or Ffa) -> Ua (written)
-  int adj_iteration(spd_ctx* C, int mode, const double* Uin, int Tu, int Teff) {
-    const Geo& g = C->geo;
-    if (int r = traces_of(C, Uin, Tu, Teff)) return r;
-    {
-      ProfScope ps_(C, "k_adj_interior");
-      k_adj_interior<D, P><<<blocks_for(g.Nc * Teff, 64), 64, 0, C->stream>>>(
-          C->ops, g, mode, Teff, Uin, Tu, C->dudt_a, C->Ffa[0], C->Ffa[1], C->Ffa[2], C->Ua, C->Ea[0], C->Ea[1],
-          C->Ea[2]);
-    }
-    CKL();
-    for (int d = 0; d < D; ++d) {
-      CK(cudaMemsetAsync(C->Tra[d], 0, sizeof(double) * 2 * k::V * g.T * k::NJ * g.Nc, C->stream));
-      const long long tot = (long long)Teff * k::NJ * n_iface(g, d);
-      ProfScope ps_(C, "k_adj_riemann");
-      k_adj_riemann<D, P><<<blocks_for(tot, 64), 64, 0, C->stream>>>(g, d, Teff, C->cfg.riemann_solver_sd,
-                                                                    C->trace[d], C->bcfix[d], C->Ea[d], C->Tra[d]);
-      CKL();
-    }
-    {
-      ProfScope ps_(C, "k_adj_traces");
-      k_adj_traces<D, P><<<blocks_for(g.Nc * Teff, 128), 128, 0, C->stream>>>(C->ops, g, Teff, C->Tra[0], C->Tra[1],
-                                                                             C->Tra[2], C->Ua);
-    }
-    CKL();
-    return 0;
-  }
-
-  int vjp(spd_ctx* C) override {
-    const Geo& g = C->geo;
-    const spd_config& cf = C->cfg;
-    const int m = C->T - 1;
-    const long long nsp = (long long)k::V * k::NS * g.Nc;
-    const size_t nader = (size_t)k::V * C->T * k::NS * g.Nc;
-    int final_mode = 1;
-    if (cf.update == SPD_UPDATE_FV) {
-      final_mode = 2;
-      long long nface[3] = {1, 1, 1};
-      size_t per = 0;
-      for (int d = 0; d < D; ++d) {
-        nface[d] = n_faces(g, d);
-        per += (size_t)nface[d];
-        CK(cudaMemsetAsync(C->FHa[d], 0, sizeof(double) * C->T * k::V * nface[d], C->stream));
-      }
-      {
-        ProfScope ps_(C, "k_adj_cv_to_sp");
-        k_adj_cv_to_sp<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_cv_to_sp, C->Usp_a,
-                                                                                 C->Unew_a);
-      }
-      CKL();
-      CK(cudaMemsetAsync(C->Usp_a, 0, sizeof(double) * nsp, C->stream));
-      if (cf.FB) {
-        CK(cudaMemsetAsync(C->W_a, 0, sizeof(double) * k::V * g.Nqe, C->stream));
-        // fixed-state ghost sides read the boundary buffers, which no step overwrites
-        for (int d = 0; d < D; ++d) {
-          const int o0 = (d == 0) ? 1 : 0;
-          const int o1 = (d == 2) ? 1 : 2;
-          CK(cudaMemcpyAsync(C->bcbuf_a[d], C->bcbuf[d], sizeof(double) * 2 * k::V * NGH * g.Xe[o0] * g.Xe[o1],
-                             cudaMemcpyDeviceToDevice, C->stream));
-        }
-      }
-      for (int i = C->T - 1; i >= 0; --i) {
-        const double w_i = C->ops.w_tp[i];
-        const double* Ucv_i = C->hist_ucv + (size_t)i * k::V * g.Nq;
-        size_t off = 0;
-        for (int d = 0; d < D; ++d) {
-          const double* aff = cf.FB ? C->hist_aff + (size_t)i * per + off : nullptr;
-          ProfScope ps_(C, "k_adj_faces");
-          k_adj_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(
-              g, C->fvg, d, C->hist_dt, w_i, cf.FB ? 1 : 0, cf.godunov, aff, C->Unew_a,
-              C->FHa[d] + (size_t)i * k::V * nface[d], C->Fba[d]);
-          CKL();
-          off += (size_t)nface[d];
-        }
-        if (cf.FB) {
-          {
-            ProfScope ps_(C, "k_prim_ext");
-            k_prim_ext<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, Ucv_i, C->W_ext);
-          }
-          CKL();
-          for (int d = 0; d < D; ++d) {
-            const int o0 = (d == 0) ? 1 : 0;
-            const int o1 = (d == 2) ? 1 : 2;
-            const long long tot = 2LL * k::V * NGH * g.Xe[o0] * g.Xe[o1];
-            ProfScope ps_(C, "k_ghost");
-            k_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, 1, k::V, k::V, C->W_ext, C->bcbuf_a[d],
-                                                                  nullptr);
-            CKL();
-          }
-          const double* affd[3] = {nullptr, nullptr, nullptr};
-          off = 0;
-          for (int d = 0; d < D; ++d) {
-            affd[d] = C->hist_aff + (size_t)i * per + off;
-            off += (size_t)nface[d];
-            ProfScope ps_(C, "k_adj_muscl_riemann");
-            k_adj_muscl_riemann<D><<<blocks_for(nface[d], 64), 64, 0, C->stream>>>(
-                g, C->fvg, d, cf.riemann_solver_fv, cf.slope_limiter, cf.godunov, C->hist_dt, w_i, affd[d], C->W_ext,
-                C->Fba[d], C->FA[d]);
-            CKL();
-          }
-          {
-            ProfScope ps_(C, "k_adj_muscl_cells");
-            k_adj_muscl_cells<D><<<blocks_for(g.Nqe, 64), 64, 0, C->stream>>>(
-                g, C->fvg, cf.slope_limiter, cf.godunov, C->hist_dt, w_i, affd[0], affd[1], affd[2], C->FA[0],
-                C->FA[1], C->FA[2], C->W_ext, C->W_a, C->LA);
-          }
-          CKL();
-          {
-            ProfScope ps_(C, "k_adj_muscl_gather");
-            k_adj_muscl_gather<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, C->LA, C->W_a);
-          }
-          CKL();
-          for (int d = D - 1; d >= 0; --d) {
-            const int o0 = (d == 0) ? 1 : 0;
-            const int o1 = (d == 2) ? 1 : 2;
-            const long long tot = (long long)k::V * NGH * g.Xe[o0] * g.Xe[o1];
-            for (int side = 0; side < 2; ++side) {
-              ProfScope ps_(C, "k_adj_ghost");
-              k_adj_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, side, C->W_a);
-              CKL();
-            }
-          }
-        }
-        {
-          ProfScope ps_(C, "k_adj_prim_cv");
-          k_adj_prim_cv<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, Ucv_i, C->Unew_a, C->W_a, C->Ucv_a);
-        }
-        CKL();
-        std::swap(C->Ucv_a, C->Unew_a);  // the adjoint of this substep's input feeds the previous one
-      }
-      {
-        ProfScope ps_(C, "k_adj_sp_to_cv");
-        k_adj_sp_to_cv<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_sp_to_cv, C->Unew_a,
-                                                                                  C->Usp_a);
-      }
-      CKL();
-      for (int d = 0; d < D; ++d) {
-        ProfScope ps_(C, "k_adj_integrate_faces");
-        k_adj_integrate_faces<D, P><<<blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->stream>>>(C->ops, g, d,
-                                                                                                C->FHa[d], C->Ffa[d]);
-        CKL();
-      }
-    } else {
-      ProfScope ps_(C, "k_adj_sd_update");
-      k_adj_sd_update<D, P><<<blocks_for(nsp, BS), BS, 0, C->stream>>>(C->ops, g, C->hist_dt, C->Usp_a, C->dudt_a,
-                                                                       m == 0 ? 1 : C->T);
-      CKL();
-    }
-    // predictor iterations, last to first
-    for (int it = m; it >= 0; --it) {
-      const int mode = (it == m) ? final_mode : 0;
-      if (it < m) {
-        ProfScope ps_(C, "k_adj_picard");
-        k_adj_picard<D, P><<<blocks_for(nsp, BS), BS, 0, C->stream>>>(C->ops, g, C->hist_dt, C->Ua, C->Usp_a, C->dudt_a,
-                                                                      it == 0 ? 1 : 0);
-        CKL();
-      }
-      const double* Uin = (it == 0) ? C->hist_usp : C->hist_ader + (size_t)(it - 1) * nader;
-      const int Tu = (it == 0) ? 1 : C->T;
-      const int Teff = (it == 0) ? 1 : C->T;
-      if (int r = adj_iteration(C, mode, Uin, Tu, Teff)) return r;
-      if (it == 0) {
-        ProfScope ps_(C, "k_adj_add_first");
-        k_adj_add_first<D, P><<<blocks_for(nsp, BS), BS, 0, C->stream>>>(g, C->Ua, C->Usp_a);
-        CKL();
-      }
-    }
-    return 0;
-  }
+  // adjoint of the recorded step (spd_adjoint_exec.cuh, compiled in its own
+  // translation units)
+  int vjp(spd_ctx* C) override { return adjoint_vjp<D, P>(C); }
 
   int update(spd_ctx* C) override {
     const int final_mode = (C->cfg.update == SPD_UPDATE_SD) ? 1 : 2;
