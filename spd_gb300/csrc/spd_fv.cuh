@@ -607,40 +607,8 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
   }
 }
 
-// W_cv = prim(U_cv) and the CFL maximum of d*c_s + sum |v|
-// (src/sdader_simulator.py:376, src/sd_simulator.py:214-227)
-template <int D>
-__global__ void k_wcv_cmax(Geo g, const double* __restrict__ U_cv, double* __restrict__ W_cv,
-                           unsigned long long* __restrict__ cmax_bits, int* __restrict__ nan_flag) {
-  constexpr int V = D + 2, P_ = D + 1;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  double cval = 0.0;
-  bool isnan_c = false;
-  if (q < g.Nq) {
-    double u[V], W[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
-    prim<D>(u, W, g.gamma, 0);
-#pragma unroll
-    for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
-    double c = sound_speed(W[P_], W[0], g.gamma, g.min_c2) * (double)D;
-#pragma unroll
-    for (int v = 1; v <= D; ++v) c = c + abs_bits(W[v]);
-    if (c != c) isnan_c = true;
-    else cval = c;
-  }
-  // warp max then one atomic per warp
-  for (int off = 16; off > 0; off >>= 1) {
-    const double o = __shfl_down_sync(0xffffffffu, cval, off);
-    cval = (o > cval) ? o : cval;
-  }
-  const unsigned nb = __ballot_sync(0xffffffffu, isnan_c);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(cmax_bits, (unsigned long long)__double_as_longlong(cval));
-    if (nb) atomicOr(nan_flag, 1);
-  }
-}
-
+// dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when
+// a NaN entered the reduction) (src/sd_simulator.py:214-227)
 static __global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
                            double* dt) {
   const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
