@@ -316,15 +316,20 @@ def ours(args):
     W_host[...] = s.dm.W_cv
     out = torch.empty(int(np.prod(shape_u)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape_u)
     e2e_steps = max(1, min(args.steps, 5))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         s._ctx.upload("U_sp", U_host)
         s._ctx.upload("W_cv", W_host)
         s.compute_dt()
         s.perform_update()
         s._ctx.check(s._ctx.lib.spd_download(s._ctx.h, 0, out.ctypes.data_as(
             __import__("ctypes").POINTER(__import__("ctypes").c_double)), out.size), "download")
+
+    e2e_step()  # untimed: first use of the transfer staging buffer
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": dof * e2e_steps * world / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(U_host.nbytes + W_host.nbytes), "d2h_bytes_per_step": int(out.nbytes),
@@ -470,7 +475,7 @@ def adjoint_arm(args):
     s._ctx.end_sim()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    s.time, done = s._ctx.step(nsteps, 0.0, 0, s.time)
+    s.time, done, _ = s._ctx.step(nsteps, 0.0, 0, s.time)
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     results = []

@@ -6,8 +6,9 @@
  * interface is the Python class SDADER_Simulator
  * (src/sdader_simulator.py:14).  Each entry point below replaces one method
  * of that class; the Python package spd_gb300 binds them with ctypes and
- * keeps the class surface.  All arrays crossing this boundary are host
- * FP64 arrays in the reference's C-order layouts:
+ * keeps the class surface.  All arrays crossing this boundary are FP64
+ * arrays in the reference's C-order layouts (host arrays; U_sp, U_cv, W_cv
+ * and the adjoint field may also be device arrays):
  *
  *   U_sp, U_cv, W_cv   (V, Nz, Ny, Nx, nz, ny, nx)          SD layout
  *   troubles           (1, Z, Y, X)                         Z = Nz*(p+1) ...
@@ -133,7 +134,9 @@ int spd_perform_update(spd_ctx* ctx, double* time_inout);
  * perform_time_evolution (:401-413), without init_sim / end_sim.
  * mode 0: n_step iterations of (compute_dt, perform_update);
  * mode 1: advance while *time_inout < t_end with the t_end clip and the
- *         dt < 1e-14 stop.  *nsteps_done receives the steps taken. */
+ *         dt < 1e-14 stop.  *nsteps_done receives the steps taken.
+ * A non-finite dt does not stop the loop (the reference runs on with it);
+ * the call then returns SPD_ERR_NONFINITE with the steps done. */
 int spd_step(spd_ctx* ctx, int nsteps, double t_end, int mode, double* time_inout, int* nsteps_done);
 /* SDADER_Simulator.end_sim (:385-392): U_cv = sp_to_cv(U_sp), W_cv = prim(U_cv). */
 int spd_end_sim(spd_ctx* ctx);

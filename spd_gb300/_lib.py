@@ -220,11 +220,13 @@ class Context:
         return t.value
 
     def step(self, nsteps: int, t_end: float, mode: int, time: float):
+        """Returns (time, steps done, True when a dt was not finite)."""
         t = ctypes.c_double(time)
         done = ctypes.c_int(0)
-        self.check(self.lib.spd_step(self.h, int(nsteps), float(t_end), int(mode), ctypes.byref(t),
-                                     ctypes.byref(done)), "step")
-        return t.value, done.value
+        rc = self.lib.spd_step(self.h, int(nsteps), float(t_end), int(mode), ctypes.byref(t), ctypes.byref(done))
+        if rc != SPD_ERR_NONFINITE:
+            self.check(rc, "step")
+        return t.value, done.value, rc == SPD_ERR_NONFINITE
 
     def end_sim(self):
         self.check(self.lib.spd_end_sim(self.h), "end_sim")

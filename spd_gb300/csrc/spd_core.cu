@@ -538,10 +538,12 @@ int spd_perform_update(spd_ctx* C, double* time_inout) {
 int spd_step(spd_ctx* C, int nsteps, double t_end, int mode, double* time_inout, int* nsteps_done) {
   if (!C || !time_inout) return SPD_ERR_ARG;
   int done = 0;
+  bool nonfinite = false;
   if (mode == 0) {
     for (int i = 0; i < nsteps; ++i) {
       if (int r = C->stepper->cmax(C)) return r;
       if (int r = spd_perform_update(C, time_inout)) return r;
+      nonfinite = nonfinite || !std::isfinite(*time_inout);
       ++done;
     }
   } else {
@@ -554,12 +556,14 @@ int spd_step(spd_ctx* C, int nsteps, double t_end, int mode, double* time_inout,
       }
       if (dt < 1e-14) break;
       if (int r = spd_perform_update(C, time_inout)) return r;
+      nonfinite = nonfinite || !std::isfinite(dt);
       ++done;
       if (nsteps > 0 && done >= nsteps) break;
     }
   }
   if (nsteps_done) *nsteps_done = done;
-  return SPD_OK;
+  // the steps ran as the reference runs them; the status reports the blow-up
+  return nonfinite ? fail(C, SPD_ERR_NONFINITE, "step: dt is not finite (the state holds NaN or inf)") : SPD_OK;
 }
 
 int spd_end_sim(spd_ctx* C) {

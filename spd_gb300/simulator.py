@@ -16,6 +16,8 @@ from collections import defaultdict
 from timeit import default_timer as timer
 from typing import Callable, Tuple
 
+import warnings
+
 import numpy as np
 
 from . import _lib
@@ -569,19 +571,27 @@ class SDADER_Simulator:
         if self.rank == 0:
             print(f"t={self.time}, steps taken {self.n_step}, time taken {self.execution_time}")
 
+    @staticmethod
+    def _warn_nonfinite(nonfinite: bool) -> None:
+        if nonfinite:
+            warnings.warn("non-finite dt: the state holds NaN or inf (the steps ran as in the reference)",
+                          RuntimeWarning, stacklevel=3)
+
     def perform_iterations(self, n_step: int) -> None:
         self.init_sim()
-        self.time, done = self._ctx.step(n_step, 0.0, 0, self.time)
+        self.time, done, nonfinite = self._ctx.step(n_step, 0.0, 0, self.time)
         self.n_step += done
         self.end_sim()
+        self._warn_nonfinite(nonfinite)
 
     def perform_time_evolution(self, t_end: float, nsteps=0) -> None:
         self.init_sim()
-        self.time, done = self._ctx.step(0, t_end, 1, self.time)
+        self.time, done, nonfinite = self._ctx.step(0, t_end, 1, self.time)
         self.n_step += done
         if self.time < t_end:
             print(f"dt={self.dm.dt}")
         self.end_sim()
+        self._warn_nonfinite(nonfinite)
 
     # ------------------------------------------------------------------
     # state snapshots (no counterpart in the reference, which has no
