@@ -530,10 +530,11 @@ __device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg
     const long long st = ext_stride(g, dd);
     const int cdd = ec[dd];
     const double hl = fg.hcv[dd][cdd - 1], hr = fg.hcv[dd][cdd], hm = fg.hfp[dd][cdd];
+    const double rhl = fg.rhcv[dd][cdd - 1], rhr = fg.rhcv[dd][cdd];
     for (int v = 0; v < V; ++v) {
       const double* M = W_ext + (long long)v * g.Nqe;
-      const double SL = (M[e] - M[e - st]) / hl;
-      const double SR = (M[e + st] - M[e]) / hr;
+      const double SL = div_rcp(M[e] - M[e - st], hl, rhl);
+      const double SR = div_rcp(M[e + st] - M[e], hr, rhr);
       SLs[dd][v] = SL;
       SRs[dd][v] = SR;
       dMh[dd][v] = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
@@ -578,11 +579,12 @@ __device__ __forceinline__ void muscl_cell_values(const Geo& g, const FvGeo& fg,
     const long long st = ext_stride(g, d);
     const int k = c[d];
     const double hl = fg.hcv[d][k - 1], hr = fg.hcv[d][k], hm = fg.hfp[d][k];
+    const double rhl = fg.rhcv[d][k - 1], rhr = fg.rhcv[d][k];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       const double* M = W_ext + (long long)v * g.Nqe;
-      const double SL = (M[e] - M[e - st]) / hl;
-      const double SR = (M[e + st] - M[e]) / hr;
+      const double SL = div_rcp(M[e] - M[e - st], hl, rhl);
+      const double SR = div_rcp(M[e + st] - M[e], hr, rhr);
       const double dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
       dMh[d][v] = dm;
       if (d == dsel) Sd[v] = 0.5 * dm * hm;
@@ -720,7 +722,7 @@ __global__ void k_adj_muscl_cells(Geo g, FvGeo fg, int limiter, int godunov, con
     for (int v = 0; v < V; ++v) {
       double SLa, SRa;
       limiter_vjp(limiter, SLs[dd][v], SRs[dd][v], hl, hr, hm, in_a[V + dd * V + v], SLa, SRa);
-      const double l = SLa / hl, rr = SRa / hr;
+      const double l = SLa * fg.rhcv[dd][cdd - 1], rr = SRa * fg.rhcv[dd][cdd];
       // SL = (W(e) - W(e-st)) / hl ; SR = (W(e+st) - W(e)) / hr
       own[v] = own[v] + l - rr;
       LA[((long long)(dd * 2 + 0) * V + v) * g.Nqe + e] = l;

@@ -15,14 +15,17 @@ namespace spd {
 SPD_FN double sgn0(double x) { return (x > 0.0) ? 1.0 : ((x < 0.0) ? -1.0 : 0.0); }
 
 // W = prim(U): Ua += (dW/dU)^T Wa
+// (Adjoint-only arithmetic below uses reciprocals freely: its values need
+// no bitwise match; values that decide a branch are recomputed exactly.)
 template <int D>
 SPD_FN void prim_vjp_add(const double* U, const double* Wa, double* Ua, double gamma) {
   constexpr int P_ = D + 1;
   const double r = U[0];
+  const double rr = 1.0 / r;
   double w[D + 2], ks = 0.0;
 #pragma unroll
   for (int v = 1; v <= D; ++v) {
-    w[v] = U[v] / r;
+    w[v] = U[v] * rr;
     ks += w[v] * w[v];
   }
   const double Pa = Wa[P_];
@@ -32,9 +35,9 @@ SPD_FN void prim_vjp_add(const double* U, const double* Wa, double* Ua, double g
   double ra = Wa[0] + Ka * 0.5 * ks;
 #pragma unroll
   for (int v = 1; v <= D; ++v) {
-    const double wa = Wa[v] + 2.0 * w[v] * ksa;
-    Ua[v] += wa / r;
-    ra -= wa * w[v] / r;
+    const double wa = (Wa[v] + 2.0 * w[v] * ksa) * rr;
+    Ua[v] += wa;
+    ra -= wa * w[v];
   }
   Ua[0] += ra;
 }
@@ -47,7 +50,7 @@ SPD_FN void cons_vjp_add(const double* W, const double* Ua, double* Wa, double g
   double ks = 0.0;
 #pragma unroll
   for (int v = 1; v <= D; ++v) ks += W[v] * W[v];
-  Wa[P_] += Ua[P_] / (gamma - 1.0);
+  Wa[P_] += Ua[P_] * (1.0 / (gamma - 1.0));
   const double ksa = Ua[P_] * 0.5 * r;
   double ra = Ua[0] + Ua[P_] * 0.5 * ks;
 #pragma unroll
@@ -67,7 +70,8 @@ SPD_FN void flux_vjp_add(const double* W, const double* Fa, double* Wa, double g
   double ks = 0.0;
 #pragma unroll
   for (int v = 1; v <= D; ++v) ks += W[v] * W[v];
-  const double E = P / (gamma - 1.0) + 0.5 * r * ks;
+  const double rg = 1.0 / (gamma - 1.0);
+  const double E = P * rg + 0.5 * r * ks;
   double ra = Fa[0] * u + Fa[v1] * u * u;
   double ua = Fa[0] * r + Fa[v1] * 2.0 * r * u + Fa[P_] * (E + P);
   double Pa = Fa[v1] + Fa[P_] * u;
@@ -79,7 +83,7 @@ SPD_FN void flux_vjp_add(const double* W, const double* Fa, double* Wa, double g
     ua += Fa[vt] * r * W[vt];
     Wa[vt] += Fa[vt] * r * u;
   }
-  Pa += Ea / (gamma - 1.0);
+  Pa += Ea * rg;
   ra += Ea * 0.5 * ks;
 #pragma unroll
   for (int v = 1; v <= D; ++v) Wa[v] += Ea * r * W[v];
@@ -91,12 +95,12 @@ SPD_FN void flux_vjp_add(const double* W, const double* Fa, double* Wa, double g
 // c = sound_speed(P, rho) (floored): adds dc/dP * ca, dc/drho * ca
 SPD_FN void sound_speed_vjp_add(double P, double rho, double gamma, double min_c2, double ca, double& Pa,
                                 double& ra) {
-  const double c2 = gamma * P / rho;
+  const double rr = 1.0 / rho;
+  const double c2 = div_rcp(gamma * P, rho, rr);  // the forward's quotient (decides the floor)
   if (!(c2 > min_c2)) return;
-  const double c = sqrt(c2);
-  const double c2a = ca * (0.5 / c);
-  Pa += c2a * gamma / rho;
-  ra -= c2a * c2 / rho;
+  const double c2a = ca * (0.5 / sqrt(c2));
+  Pa += c2a * gamma * rr;
+  ra -= c2a * c2 * rr;
 }
 
 // LLF / HLLC flux F(ML, MR): (MLa, MRa) = J^T Fa (written).  prims: the
@@ -148,28 +152,31 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
     const double rcL = WL[0] * (vL - sL);
     const double rcR = WR[0] * (sR - vR);
     const double den = rcR + rcL;
-    const double vstar = (rcR * vR + rcL * vL + (WL[P_] - WR[P_])) / den;
+    const double rden = 1.0 / den;
+    const double vstar = div_rcp(rcR * vR + rcL * vL + (WL[P_] - WR[P_]), den, rden);
     double phi = 1.0, Mach = 0.0, mx = 0.0;
     if (low_mach) {
       mx = np_max(fabs(vL), fabs(vR)) / cmax;
       Mach = np_min(1.0, mx);
       phi = Mach * (2.0 - Mach);
     }
-    const double Pstar = low_mach ? (rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR)) / den
-                                  : (rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR)) / den;
+    const double Pstar = low_mach ? div_rcp(rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR), den, rden)
+                                  : div_rcp(rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR), den, rden);
     int region;
     double r, vg, Pg, e, dd = 1.0;
     if (sL > 0.0) {
       region = 0; r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
     } else if (vstar > 0.0) {
       region = 1; dd = sL - vstar;
-      r = WL[0] * (sL - vL) / dd;
-      e = ((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar) / dd;
+      const double rd = 1.0 / dd;
+      r = div_rcp(WL[0] * (sL - vL), dd, rd);
+      e = div_rcp((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar, dd, rd);
       vg = vstar; Pg = Pstar;
     } else if (sR > 0.0) {
       region = 2; dd = sR - vstar;
-      r = WR[0] * (sR - vR) / dd;
-      e = ((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar) / dd;
+      const double rd = 1.0 / dd;
+      r = div_rcp(WR[0] * (sR - vR), dd, rd);
+      e = div_rcp((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar, dd, rd);
       vg = vstar; Pg = Pstar;
     } else {
       region = 3; r = WR[0]; vg = vR; Pg = WR[P_]; e = UR[P_];
@@ -205,14 +212,15 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
       const double EK = isL ? UL[P_] : UR[P_];
       const double PK = isL ? WL[P_] : WR[P_];
       // r = rho (sK - vK) / dd, dd = sK - vstar
-      double rho_a = ra * (sK - vK) / dd;
-      double sK_a = ra * rho / dd - ra * r / dd;
-      double vK_a = -ra * rho / dd;
-      vstar_a += ra * r / dd;
+      const double rdd = 1.0 / dd;
+      double rho_a = ra * (sK - vK) * rdd;
+      double sK_a = (ra * rho - ra * r) * rdd;
+      double vK_a = -ra * rho * rdd;
+      vstar_a += ra * r * rdd;
       // e = ((sK - vK) EK - PK vK + Pstar vstar) / dd
-      const double na = ea / dd;
-      sK_a += -ea * e / dd + na * EK;
-      vstar_a += ea * e / dd + na * Pstar;
+      const double na = ea * rdd;
+      sK_a += -na * e + na * EK;
+      vstar_a += na * e + na * Pstar;
       vK_a += -na * EK - na * PK;
       const double EK_a = na * (sK - vK);
       const double PK_a = -na * vK;
@@ -226,8 +234,8 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
     // Pstar = (rcR PL + rcL PR + phi rcL rcR (vL - vR)) / den
     double rcL_a = 0.0, rcR_a = 0.0, den_a = 0.0;
     {
-      const double na = Pstar_a / den;
-      den_a -= Pstar_a * Pstar / den;
+      const double na = Pstar_a * rden;
+      den_a -= na * Pstar;
       rcR_a += na * WL[P_] + na * phi * rcL * (vL - vR);
       rcL_a += na * WR[P_] + na * phi * rcR * (vL - vR);
       WLa[P_] += na * rcR;
@@ -254,8 +262,8 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
     }
     // vstar = (rcR vR + rcL vL + (PL - PR)) / den
     {
-      const double na = vstar_a / den;
-      den_a -= vstar_a * vstar / den;
+      const double na = vstar_a * rden;
+      den_a -= na * vstar;
       rcR_a += na * vR;
       rcL_a += na * vL;
       vR_a += na * rcR;
