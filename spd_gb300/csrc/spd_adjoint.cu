@@ -32,6 +32,7 @@ void select_slot(spd_ctx* C, int slot) {
   C->hist_ucv = C->rec_ucv_n ? C->rec_ucv + (size_t)slot * C->rec_ucv_n : nullptr;
   C->hist_aff = C->rec_aff_n ? C->rec_aff + (size_t)slot * C->rec_aff_n : nullptr;
   C->hist_dt = C->rec_dt + slot;
+  C->hist_mpred = C->rec_mpred_n ? C->rec_mpred + (size_t)slot * C->rec_mpred_n : nullptr;
 }
 
 }  // namespace
@@ -56,6 +57,7 @@ int spd_adjoint_enable(spd_ctx* C, int depth) {
   C->rec_ader_n = (size_t)m * V * T * NS * g.Nc;
   C->rec_ucv_n = fv ? (size_t)T * V * g.Nq : 0;
   C->rec_aff_n = fb ? (size_t)T * faces_total : 0;
+  C->rec_mpred_n = fb ? (size_t)T * (1 + D) * V * g.Nqe : 0;
   if (int r = adj_alloc(C, &C->rec_usp, C->rec_usp_n * depth)) return r;
   if (C->rec_ader_n)
     if (int r = adj_alloc(C, &C->rec_ader, C->rec_ader_n * depth)) return r;
@@ -63,6 +65,8 @@ int spd_adjoint_enable(spd_ctx* C, int depth) {
     if (int r = adj_alloc(C, &C->rec_ucv, C->rec_ucv_n * depth)) return r;
   if (C->rec_aff_n)
     if (int r = adj_alloc(C, &C->rec_aff, C->rec_aff_n * depth)) return r;
+  if (C->rec_mpred_n)
+    if (int r = adj_alloc(C, &C->rec_mpred, C->rec_mpred_n * depth)) return r;
   if (int r = adj_alloc(C, &C->rec_dt, (size_t)depth)) return r;
   if (int r = adj_alloc(C, &C->Usp_a, (size_t)V * NS * g.Nc)) return r;
   CK(cudaMemset(C->Usp_a, 0, sizeof(double) * V * NS * g.Nc));

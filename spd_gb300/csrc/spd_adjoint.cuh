@@ -562,60 +562,15 @@ __device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg
   for (int v = 0; v < V; ++v) pr[v] = w[v] + 0.5 * dtW[v] * dti;
 }
 
-// The forward's half-step prediction and direction-dd slope term of
-// extended cell e (k_muscl_cells arithmetic, values only).
-template <int D>
-__device__ __forceinline__ void muscl_cell_values(const Geo& g, const FvGeo& fg, int limiter, double dti, long long e,
-                                                  int dsel, const double* __restrict__ W_ext, double* pred,
-                                                  double* Sd) {
-  constexpr int V = D + 2, P_ = D + 1;
-  int c[3];
-  e_coords(g, e, c[0], c[1], c[2]);
-  double W[V], dMh[D][V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) W[v] = W_ext[(long long)v * g.Nqe + e];
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const long long st = ext_stride(g, d);
-    const int k = c[d];
-    const double hl = fg.hcv[d][k - 1], hr = fg.hcv[d][k], hm = fg.hfp[d][k];
-    const double rhl = fg.rhcv[d][k - 1], rhr = fg.rhcv[d][k];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const double* M = W_ext + (long long)v * g.Nqe;
-      const double SL = div_rcp(M[e] - M[e - st], hl, rhl);
-      const double SR = div_rcp(M[e + st] - M[e], hr, rhr);
-      const double dm = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
-      dMh[d][v] = dm;
-      if (d == dsel) Sd[v] = 0.5 * dm * hm;
-    }
-  }
-  double dtW[V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) dtW[v] = 0.0;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const int vel = d + 1;
-    const double* dW = dMh[d];
-    dtW[0] = dtW[0] - (W[vel] * dW[0] + W[0] * dW[vel]);
-    dtW[P_] = dtW[P_] - (W[vel] * dW[P_] + g.gamma * W[P_] * dW[vel]);
-    dtW[vel] = dtW[vel] - (W[vel] * dW[vel] + dW[P_] / W[0]);
-#pragma unroll
-    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - W[vel] * dW[v2];
-  }
-  dtW[P_] = dtW[P_] * 0.0;
-#pragma unroll
-  for (int v = 0; v < V; ++v) pred[v] = W[v] + 0.5 * dtW[v] * dti;
-}
-
 // MUSCL-Hancock adjoint, phase 1: on every face of direction d whose
 // fallback flux was used, the Riemann VJP of Fb_a onto the two
-// reconstructed states, FA[side][v][face] (side 0 = left state).
+// reconstructed states, FA[side][v][face] (side 0 = left state).  The
+// states are the recorded forward's predictions and slope terms
+// (Mpred [v][e], S [dir][v][e]; valid on the cells of used faces).
 template <int D>
-__global__ void k_adj_muscl_riemann(Geo g, FvGeo fg, int d, int solver, int limiter, int godunov,
-                                    const double* __restrict__ dt_ptr, double w_i, const double* __restrict__ aff,
-                                    const double* __restrict__ W_ext, const double* __restrict__ Fba,
-                                    double* __restrict__ FA) {
+__global__ void k_adj_muscl_riemann(Geo g, int d, int solver, int godunov, const double* __restrict__ aff,
+                                    const double* __restrict__ Mpred, const double* __restrict__ S,
+                                    const double* __restrict__ Fba, double* __restrict__ FA) {
   constexpr int V = D + 2;
   const long long nf = n_faces(g, d);
   const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -631,13 +586,12 @@ __global__ void k_adj_muscl_riemann(Geo g, FvGeo fg, int d, int solver, int limi
   for (int kk = 0; kk < 3; ++kk) e1c[kk] = (kk < D) ? f[kk] + NGH : 0;
   e1c[d] = f[d] + 1;
   const long long e1 = e1c[0] + (long long)g.Xe[0] * (e1c[1] + (long long)g.Xe[1] * e1c[2]);
-  const long long ecell[2] = {e1, e1 + ext_stride(g, d)};
-  const double dti = *dt_ptr * w_i;
+  const long long e2 = e1 + ext_stride(g, d);
   double M[2][V];
-  for (int side = 0; side < 2; ++side) {
-    double pred[V], Sd[V];
-    muscl_cell_values<D>(g, fg, limiter, dti, ecell[side], d, W_ext, pred, Sd);
-    for (int v = 0; v < V; ++v) M[side][v] = (side == 0) ? pred[v] + Sd[v] : pred[v] - Sd[v];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    M[0][v] = Mpred[(long long)v * g.Nqe + e1] + S[((long long)d * V + v) * g.Nqe + e1];
+    M[1][v] = Mpred[(long long)v * g.Nqe + e2] - S[((long long)d * V + v) * g.Nqe + e2];
   }
   double Fa[V], MLa[V], MRa[V];
   for (int v = 0; v < V; ++v) Fa[v] = Fba[(long long)v * nf + fidx];

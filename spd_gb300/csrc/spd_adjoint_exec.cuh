@@ -120,9 +120,9 @@ int adjoint_vjp(spd_ctx* C) {
           affd[d] = C->hist_aff + (size_t)i * per + off;
           off += (size_t)nface[d];
           ProfScope ps_(C, "k_adj_muscl_riemann");
+          const double* mp = C->hist_mpred + (size_t)i * (1 + D) * k::V * g.Nqe;
           k_adj_muscl_riemann<D><<<blocks_for(nface[d], 64), 64, 0, C->stream>>>(
-              g, C->fvg, d, cf.riemann_solver_fv, cf.slope_limiter, cf.godunov, C->hist_dt, w_i, affd[d], C->W_ext,
-              C->Fba[d], C->FA[d]);
+              g, d, cf.riemann_solver_fv, cf.godunov, affd[d], mp, mp + (size_t)k::V * g.Nqe, C->Fba[d], C->FA[d]);
           CKL();
         }
         {

@@ -46,13 +46,15 @@ struct spd_ctx {
   double* tape_aff = nullptr;
   int adj_depth = 0;
   std::vector<void*> adj_allocs;
-  size_t rec_usp_n = 0, rec_ader_n = 0, rec_ucv_n = 0, rec_aff_n = 0;
+  size_t rec_usp_n = 0, rec_ader_n = 0, rec_ucv_n = 0, rec_aff_n = 0, rec_mpred_n = 0;
   double *rec_usp = nullptr, *rec_ader = nullptr, *rec_ucv = nullptr, *rec_aff = nullptr, *rec_dt = nullptr;
+  double* rec_mpred = nullptr;
   double* hist_usp = nullptr;   // U_sp at the start of the recorded step
   double* hist_ader = nullptr;  // U_ader after each Picard iteration but the last (m slots)
   double* hist_ucv = nullptr;   // U_cv at the start of each FV substep (T slots)
   double* hist_aff = nullptr;   // affected faces of each substep (T slots, all directions)
   double* hist_dt = nullptr;    // dt of the recorded step
+  double* hist_mpred = nullptr; // MUSCL-Hancock predictions and slope terms of each substep (T slots)
   double* Usp_a = nullptr;
   double* Ua = nullptr;
   double* dudt_a = nullptr;

@@ -289,6 +289,12 @@ struct Stepper : StepperBase {
         }
         k_muscl_cells_grid(C, w_i, i);
         CKL();
+        if (C->recording) {
+          const size_t nq = (size_t)k::V * g.Nqe;
+          double* dst = C->hist_mpred + (size_t)i * (1 + D) * nq;
+          CK(cudaMemcpyAsync(dst, C->Mpred, sizeof(double) * nq, cudaMemcpyDeviceToDevice, C->stream));
+          CK(cudaMemcpyAsync(dst + nq, C->S, sizeof(double) * D * nq, cudaMemcpyDeviceToDevice, C->stream));
+        }
         for (int d = 0; d < D; ++d) {
           {
             ProfScope ps_(C, "k_muscl_faces");
