@@ -256,6 +256,25 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
+# multi-process bookkeeping (replicas: one process per GPU, no collective on
+# the data path; the slowest rank's time defines the job's time)
+# ---------------------------------------------------------------------------
+def max_over_ranks(ms, dist, device):
+    """The maximum of ``ms`` over all ranks (``dist`` None: single process)."""
+    if dist is None:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step, steps, world, ms):
+    """Units processed by all ranks per second over the slowest rank's time."""
+    return units_per_rank_step * steps * world / (ms / 1e3)
+
+
+# ---------------------------------------------------------------------------
 # the GPU arm
 # ---------------------------------------------------------------------------
 def ours(args):
@@ -296,16 +315,13 @@ def ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     ctx.profile(False)
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     launches = ctx.launch_count() - launches0
     prof = ctx.profile_report()
     clocks = clk.summary()
-    value = dof * args.steps * world / (ms / 1e3)
+    value = whole_job_rate(dof, args.steps, world, ms)
 
     # end to end through the public API with host buffers
     shape_u = s._shape_of("U_sp")
@@ -631,6 +647,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload in ("kh_ensemble", "kh_ensemble_small", "kh_adjoint") and int(os.environ.get("RANK", "0")):
+        return  # these workloads run on one GPU: under torchrun only rank 0 runs them
     elif args.workload in ("kh_ensemble", "kh_ensemble_small"):
         from spd_gb300.build import build
         build()
