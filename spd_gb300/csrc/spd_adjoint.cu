@@ -75,6 +75,7 @@ int spd_adjoint_enable(spd_ctx* C, int depth) {
   for (int d = 0; d < D; ++d) {
     if (int r = adj_alloc(C, &C->Ea[d], (size_t)2 * V * T * NJ * g.Nc)) return r;
     if (int r = adj_alloc(C, &C->Tra[d], (size_t)2 * V * T * NJ * g.Nc)) return r;
+    if (int r = adj_alloc(C, &C->Upart[d], (size_t)V * T * NS * g.Nc)) return r;
     if (fv) {
       if (int r = adj_alloc(C, &C->Ffa[d], (size_t)V * T * NJ * C->nf * g.Nc)) return r;
       if (int r = adj_alloc(C, &C->FHa[d], (size_t)T * V * nface[d])) return r;

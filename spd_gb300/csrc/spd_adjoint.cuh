@@ -17,91 +17,94 @@ namespace spd {
 // ---------------------------------------------------------------------------
 // predictor
 // ---------------------------------------------------------------------------
-// Adjoint of one fused interior kernel launch (k_interior) for cell c and
-// time node t.  Input: the adjoint of dudt (mode 0/1) or of the flux points
-// (mode 2).  Output: Ua (adjoint of this iteration's U_ader[t] from the
-// interior flux points, written, not added) and the edge adjoints Ea.
+// Adjoint of one fused interior kernel launch (k_interior), one thread per
+// (cell c, time node t, direction d, transverse line j).  Input: the
+// adjoint of dudt (mode 0/1) or of the flux points (mode 2).  Output: the
+// line's share of the adjoint of this iteration's input U[t] (Upart[d],
+// written; each point of a cell lies on exactly one line per direction)
+// and the edge adjoints Ea of the line.
 template <int D, int P>
 __global__ void k_adj_interior(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
                                const double* __restrict__ dudt_a, const double* Ffa0, const double* Ffa1,
-                               const double* Ffa2, double* __restrict__ Ua, double* Ea0, double* Ea1, double* Ea2) {
+                               const double* Ffa2, double* Up0, double* Up1, double* Up2, double* Ea0, double* Ea1,
+                               double* Ea2) {
   using k = K<D, P>;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (tid >= g.Nc * Teff) return;
-  const long long c = tid % g.Nc;
-  const int t = (int)(tid / g.Nc);
+  const unsigned nc = (unsigned)g.Nc;
+  if (tid >= (long long)nc * Teff * D * k::NJ) return;
+  const unsigned ut = (unsigned)tid;
+  const unsigned c = ut % nc;
+  unsigned rest = ut / nc;
+  const int j = (int)(rest % k::NJ);
+  rest /= k::NJ;
+  const int d = (int)(rest % D);
+  const int t = (int)(rest / D);
   const int tu = (Tu == 1) ? 0 : t;
-  const double* Ffa[3] = {Ffa0, Ffa1, Ffa2};
-  double* Ea[3] = {Ea0, Ea1, Ea2};
-  double acc[k::V][k::NS];
+  const double* Ffa = (d == 0) ? Ffa0 : (d == 1 ? Ffa1 : Ffa2);
+  double* Up = (d == 0) ? Up0 : (d == 1 ? Up1 : Up2);
+  double* Ea = (d == 0) ? Ea0 : (d == 1 ? Ea1 : Ea2);
+  double Fla[k::V][k::nf];
+  if (mode == 2) {
+#pragma unroll
+    for (int v = 0; v < k::V; ++v)
+#pragma unroll
+      for (int f = 0; f < k::nf; ++f) Fla[v][f] = Ffa[((((long long)v * g.T + t) * k::NJ + j) * k::nf + f) * nc + c];
+  } else {
+    // derivative transpose: val = (sum_f dfp_to_sp[so][f] F[f]) / h
+    const double rh = 1.0 / g.h[d];
+#pragma unroll
+    for (int v = 0; v < k::V; ++v) {
+#pragma unroll
+      for (int f = 0; f < k::nf; ++f) Fla[v][f] = 0.0;
+#pragma unroll
+      for (int so = 0; so < k::n; ++so) {
+        const int s = sp_index<D, P>(d, j, so);
+        const double da = dudt_a[(((long long)v * g.T + t) * k::NS + s) * nc + c] * rh;
+#pragma unroll
+        for (int f = 0; f < k::nf; ++f) Fla[v][f] += op.dfp_to_sp[so * k::nf + f] * da;
+      }
+    }
+  }
+  // edge flux points: adjoint of the interface fluxes
+#pragma unroll
+  for (int v = 0; v < k::V; ++v) {
+    Ea[(((long long)(0 * k::V + v) * g.T + t) * k::NJ + j) * nc + c] = Fla[v][0];
+    Ea[(((long long)(1 * k::V + v) * g.T + t) * k::NJ + j) * nc + c] = Fla[v][k::nf - 1];
+  }
+  // interior flux points
+  double u[k::V][k::n], acc[k::V][k::n];
 #pragma unroll
   for (int v = 0; v < k::V; ++v)
 #pragma unroll
-    for (int s = 0; s < k::NS; ++s) acc[v][s] = 0.0;
-  for (int d = 0; d < D; ++d) {
-    for (int j = 0; j < k::NJ; ++j) {
-      double Fla[k::V][k::nf];
-      if (mode == 2) {
-#pragma unroll
-        for (int v = 0; v < k::V; ++v)
-#pragma unroll
-          for (int f = 0; f < k::nf; ++f)
-            Fla[v][f] = Ffa[d][((((long long)v * g.T + t) * k::NJ + j) * k::nf + f) * g.Nc + c];
-      } else {
-        // derivative transpose: val = (sum_f dfp_to_sp[so][f] F[f]) / h
-#pragma unroll
-        for (int v = 0; v < k::V; ++v) {
-#pragma unroll
-          for (int f = 0; f < k::nf; ++f) Fla[v][f] = 0.0;
-#pragma unroll
-          for (int so = 0; so < k::n; ++so) {
-            const int s = sp_index<D, P>(d, j, so);
-            const double da = dudt_a[(((long long)v * g.T + t) * k::NS + s) * g.Nc + c] / g.h[d];
-#pragma unroll
-            for (int f = 0; f < k::nf; ++f) Fla[v][f] += op.dfp_to_sp[so * k::nf + f] * da;
-          }
-        }
-      }
-      // edge flux points: adjoint of the interface fluxes
-#pragma unroll
-      for (int v = 0; v < k::V; ++v) {
-        Ea[d][(((long long)(0 * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + c] = Fla[v][0];
-        Ea[d][(((long long)(1 * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + c] = Fla[v][k::nf - 1];
-      }
-      // interior flux points
-      double u[k::V][k::n];
-#pragma unroll
-      for (int v = 0; v < k::V; ++v)
-#pragma unroll
-        for (int s = 0; s < k::n; ++s)
-          u[v][s] = Uin[(((long long)v * Tu + tu) * k::NS + sp_index<D, P>(d, j, s)) * g.Nc + c];
-#pragma unroll
-      for (int f = 1; f < k::nf - 1; ++f) {
-        double M[k::V], Fa[k::V], Ma[k::V];
-#pragma unroll
-        for (int v = 0; v < k::V; ++v) {
-          M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
-          Fa[v] = Fla[v][f];
-        }
-        {
-          double W[k::V], Wa[k::V];
-          prim<D>(M, W, g.gamma, 0);
-#pragma unroll
-          for (int v = 0; v < k::V; ++v) { Wa[v] = 0.0; Ma[v] = 0.0; }
-          flux_vjp_add<D>(W, Fa, Wa, g.gamma, d);
-          prim_vjp_add<D>(M, Wa, Ma, g.gamma);
-        }
-#pragma unroll
-        for (int v = 0; v < k::V; ++v)
-#pragma unroll
-          for (int s = 0; s < k::n; ++s) acc[v][sp_index<D, P>(d, j, s)] += op.sp_to_fp[f * k::n + s] * Ma[v];
-      }
+    for (int s = 0; s < k::n; ++s) {
+      u[v][s] = Uin[(((long long)v * Tu + tu) * k::NS + sp_index<D, P>(d, j, s)) * nc + c];
+      acc[v][s] = 0.0;
     }
+#pragma unroll
+  for (int f = 1; f < k::nf - 1; ++f) {
+    double M[k::V], W[k::V], Wa[k::V], Ma[k::V];
+#pragma unroll
+    for (int v = 0; v < k::V; ++v) {
+      M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
+      Wa[v] = 0.0;
+      Ma[v] = 0.0;
+    }
+    prim<D>(M, W, g.gamma, 0);
+    double Fa[k::V];
+#pragma unroll
+    for (int v = 0; v < k::V; ++v) Fa[v] = Fla[v][f];
+    flux_vjp_add<D>(W, Fa, Wa, g.gamma, d);
+    prim_vjp_add<D>(M, Wa, Ma, g.gamma);
+#pragma unroll
+    for (int v = 0; v < k::V; ++v)
+#pragma unroll
+      for (int s = 0; s < k::n; ++s) acc[v][s] += op.sp_to_fp[f * k::n + s] * Ma[v];
   }
 #pragma unroll
   for (int v = 0; v < k::V; ++v)
 #pragma unroll
-    for (int s = 0; s < k::NS; ++s) Ua[(((long long)v * Teff + t) * k::NS + s) * g.Nc + c] = acc[v][s];
+    for (int s = 0; s < k::n; ++s)
+      Up[(((long long)v * Teff + t) * k::NS + sp_index<D, P>(d, j, s)) * nc + c] = acc[v][s];
 }
 
 // Adjoint of the element-interface Riemann fluxes of direction d: the
@@ -214,30 +217,41 @@ __global__ void k_adj_riemann(Geo g, int d, int Teff, int solver, const double* 
   }
 }
 
-// Ua[t] += (edge traces)^T Tra for cell c and node t (Ua written by
-// k_adj_interior of the same iteration).
+// Ua[t] = sum over directions of the interior partials (Upart, from
+// k_adj_interior) + (edge traces)^T Tra, for cell c and node t; one thread
+// per (cell, node, direction-d line j), adding in a fixed order.
 template <int D, int P>
 __global__ void k_adj_traces(Ops op, Geo g, int Teff, const double* __restrict__ Tra0, const double* Tra1,
-                             const double* Tra2, double* __restrict__ Ua) {
+                             const double* Tra2, const double* Up0, const double* Up1, const double* Up2,
+                             double* __restrict__ Ua) {
   using k = K<D, P>;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (tid >= g.Nc * Teff) return;
-  const long long c = tid % g.Nc;
-  const int t = (int)(tid / g.Nc);
+  const unsigned nc = (unsigned)g.Nc;
+  if (tid >= (long long)nc * Teff * k::NS) return;
+  const unsigned ut = (unsigned)tid;
+  const unsigned c = ut % nc;
+  const unsigned rest = ut / nc;
+  const int s = (int)(rest % k::NS);
+  const int t = (int)(rest / k::NS);
   const double* Tra[3] = {Tra0, Tra1, Tra2};
-  for (int d = 0; d < D; ++d) {
-    for (int j = 0; j < k::NJ; ++j) {
+  const double* Up[3] = {Up0, Up1, Up2};
+  // coordinates of point s: index along each direction and transverse line
+  const int kx = s % k::n, ky = (s / k::n) % k::n, kz = s / (k::n * k::n);
 #pragma unroll
-      for (int v = 0; v < k::V; ++v) {
-        const double l = Tra[d][(((long long)(0 * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + c];
-        const double r = Tra[d][(((long long)(1 * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + c];
+  for (int v = 0; v < k::V; ++v) {
+    const long long ui = (((long long)v * Teff + t) * k::NS + s) * nc + c;
+    double a = Up[0][ui];
 #pragma unroll
-        for (int s = 0; s < k::n; ++s) {
-          double* u = &Ua[(((long long)v * Teff + t) * k::NS + sp_index<D, P>(d, j, s)) * g.Nc + c];
-          *u += op.sp_to_fp[s] * l + op.sp_to_fp[(k::nf - 1) * k::n + s] * r;
-        }
-      }
+    for (int d = 1; d < D; ++d) a += Up[d][ui];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const int kd = (d == 0) ? kx : (d == 1 ? ky : kz);
+      const int j = (d == 0) ? (ky + k::n * kz) : (d == 1 ? (kx + k::n * kz) : (kx + k::n * ky));
+      const double l = Tra[d][(((long long)(0 * k::V + v) * g.T + t) * k::NJ + j) * nc + c];
+      const double r = Tra[d][(((long long)(1 * k::V + v) * g.T + t) * k::NJ + j) * nc + c];
+      a += op.sp_to_fp[kd] * l + op.sp_to_fp[(k::nf - 1) * k::n + kd] * r;
     }
+    Ua[ui] = a;
   }
 }
 

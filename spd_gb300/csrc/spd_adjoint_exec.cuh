@@ -29,9 +29,9 @@ int adj_iteration(spd_ctx* C, int mode, const double* Uin, int Tu, int Teff) {
   if (int r = adj_traces_of<D, P>(C, Uin, Tu, Teff)) return r;
   {
     ProfScope ps_(C, "k_adj_interior");
-    k_adj_interior<D, P><<<blocks_for(g.Nc * Teff, 64), 64, 0, C->stream>>>(
-        C->ops, g, mode, Teff, Uin, Tu, C->dudt_a, C->Ffa[0], C->Ffa[1], C->Ffa[2], C->Ua, C->Ea[0], C->Ea[1],
-        C->Ea[2]);
+    k_adj_interior<D, P><<<blocks_for(g.Nc * Teff * D * k::NJ, 128), 128, 0, C->stream>>>(
+        C->ops, g, mode, Teff, Uin, Tu, C->dudt_a, C->Ffa[0], C->Ffa[1], C->Ffa[2], C->Upart[0], C->Upart[1],
+        C->Upart[2], C->Ea[0], C->Ea[1], C->Ea[2]);
   }
   CKL();
   for (int d = 0; d < D; ++d) {
@@ -44,8 +44,8 @@ int adj_iteration(spd_ctx* C, int mode, const double* Uin, int Tu, int Teff) {
   }
   {
     ProfScope ps_(C, "k_adj_traces");
-    k_adj_traces<D, P><<<blocks_for(g.Nc * Teff, 128), 128, 0, C->stream>>>(C->ops, g, Teff, C->Tra[0], C->Tra[1],
-                                                                           C->Tra[2], C->Ua);
+    k_adj_traces<D, P><<<blocks_for(g.Nc * Teff * k::NS, 128), 128, 0, C->stream>>>(
+        C->ops, g, Teff, C->Tra[0], C->Tra[1], C->Tra[2], C->Upart[0], C->Upart[1], C->Upart[2], C->Ua);
   }
   CKL();
   return 0;

@@ -60,6 +60,7 @@ struct spd_ctx {
   double* dudt_a = nullptr;
   double* Ea[3] = {nullptr, nullptr, nullptr};
   double* Tra[3] = {nullptr, nullptr, nullptr};
+  double* Upart[3] = {nullptr, nullptr, nullptr};  // per-direction interior shares of Ua
   double* Ffa[3] = {nullptr, nullptr, nullptr};
   double* FHa[3] = {nullptr, nullptr, nullptr};
   double* Fba[3] = {nullptr, nullptr, nullptr};
