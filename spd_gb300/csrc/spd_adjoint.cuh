@@ -4,9 +4,9 @@
 // branches frozen at their forward values.  Linear pieces (interpolation,
 // derivative, Picard sums, subcell transforms, flux divergence, boundary
 // copies) are transposed directly; the pointwise nonlinear maps
-// (primitives, Euler flux, LLF/HLLC) use the reverse-mode products of
-// spd_vjp.cuh, and the MUSCL-Hancock half-step predictor forward-mode dual
-// numbers over its inputs.  Adjoint arrays use the forward layouts
+// (primitives, Euler flux, LLF/HLLC, the MUSCL-Hancock half-step
+// predictor) use hand-derived reverse-mode products (spd_vjp.cuh,
+// predictor_vjp).  Adjoint arrays use the forward layouts
 // (spd_kernels.cuh, spd_fv.cuh); suffix _a.
 #pragma once
 #include "spd_fv.cuh"
@@ -529,14 +529,12 @@ __device__ __forceinline__ void limiter_vjp(int limiter, double SL, double SR, d
 }
 
 // Limited gradients of extended cell e in every direction (the forward's
-// k_muscl_cells arithmetic) and the half-step prediction as duals over
-// (W(e), dMh[direction][variable]).
+// k_muscl_cells arithmetic: values and branches as in the recorded step).
 template <int D>
-__device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg, int limiter, double dti, long long e,
+__device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg, int limiter, long long e,
                                                    const double* __restrict__ W_ext, double* W, double (*SLs)[D + 2],
-                                                   double (*SRs)[D + 2], double (*dMh)[D + 2],
-                                                   Dual<(D + 2) * (1 + D)>* pr) {
-  constexpr int V = D + 2, P_ = D + 1, NT = V * (1 + D);
+                                                   double (*SRs)[D + 2], double (*dMh)[D + 2]) {
+  constexpr int V = D + 2;
   int ec[3];
   e_coords(g, e, ec[0], ec[1], ec[2]);
   for (int v = 0; v < V; ++v) W[v] = W_ext[(long long)v * g.Nqe + e];
@@ -554,26 +552,41 @@ __device__ __forceinline__ void muscl_cell_forward(const Geo& g, const FvGeo& fg
       dMh[dd][v] = (limiter == LIM_MINMOD) ? minmod(SL, SR) : moncen(SL, SR, hl, hr, hm);
     }
   }
-  Dual<NT> w[V], dm[D][V], dtW[V];
+}
+
+// Transpose of the half-step prediction pr = W + 0.5 dti dtW(W, dMh)
+// (k_muscl_cells; the pressure component of dtW is multiplied by 0):
+// in_a[0..V) += dpr/dW^T pra, in_a[V + dd V + v] += dpr/d(dMh[dd][v])^T pra.
+template <int D>
+SPD_FN void predictor_vjp(const double* W, const double (*dMh)[D + 2], double dti, const double* pra,
+                          double* in_a) {
+  constexpr int V = D + 2, P_ = D + 1;
+  double dta[V];
   for (int v = 0; v < V; ++v) {
-    w[v] = Dual<NT>(W[v]);
-    w[v].d[v] = 1.0;
+    in_a[v] += pra[v];
+    dta[v] = 0.5 * dti * pra[v];
   }
-  for (int dd = 0; dd < D; ++dd)
-    for (int v = 0; v < V; ++v) {
-      dm[dd][v] = Dual<NT>(dMh[dd][v]);
-      dm[dd][v].d[V + dd * V + v] = 1.0;
-    }
-  for (int v = 0; v < V; ++v) dtW[v] = Dual<NT>(0.0);
+  dta[P_] = 0.0;
+  const double rw0 = 1.0 / W[0];
   for (int dd = 0; dd < D; ++dd) {
     const int vel = dd + 1;
-    dtW[0] = dtW[0] - (w[vel] * dm[dd][0] + w[0] * dm[dd][vel]);
-    dtW[P_] = dtW[P_] - (w[vel] * dm[dd][P_] + g.gamma * w[P_] * dm[dd][vel]);
-    dtW[vel] = dtW[vel] - (w[vel] * dm[dd][vel] + dm[dd][P_] / w[0]);
-    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - w[vel] * dm[dd][v2];
+    double* dma = in_a + V + dd * V;
+    // dtW[0] -= W[vel] dm[0] + W[0] dm[vel]
+    in_a[vel] -= dta[0] * dMh[dd][0];
+    dma[0] -= dta[0] * W[vel];
+    in_a[0] -= dta[0] * dMh[dd][vel];
+    dma[vel] -= dta[0] * W[0];
+    // dtW[vel] -= W[vel] dm[vel] + dm[P] / W[0]
+    in_a[vel] -= dta[vel] * dMh[dd][vel];
+    dma[vel] -= dta[vel] * W[vel];
+    dma[P_] -= dta[vel] * rw0;
+    in_a[0] += dta[vel] * dMh[dd][P_] * rw0 * rw0;
+    // dtW[v2] -= W[vel] dm[v2], v2 = 2..D
+    for (int v2 = 2; v2 <= D; ++v2) {
+      in_a[vel] -= dta[v2] * dMh[dd][v2];
+      dma[v2] -= dta[v2] * W[vel];
+    }
   }
-  dtW[P_] = dtW[P_] * 0.0;
-  for (int v = 0; v < V; ++v) pr[v] = w[v] + 0.5 * dtW[v] * dti;
 }
 
 // MUSCL-Hancock adjoint, phase 1: on every face of direction d whose
@@ -672,12 +685,10 @@ __global__ void k_adj_muscl_cells(Geo g, FvGeo fg, int limiter, int godunov, con
   }
   const double dti = *dt_ptr * w_i;
   double W[V], SLs[D][V], SRs[D][V], dMh[D][V];
-  Dual<NT> pr[V];
-  muscl_cell_forward<D>(g, fg, limiter, dti, e, W_ext, W, SLs, SRs, dMh, pr);
+  muscl_cell_forward<D>(g, fg, limiter, e, W_ext, W, SLs, SRs, dMh);
   double in_a[NT];
   for (int i2 = 0; i2 < NT; ++i2) in_a[i2] = 0.0;
-  for (int v = 0; v < V; ++v)
-    for (int i2 = 0; i2 < NT; ++i2) in_a[i2] += Mpa[v] * pr[v].d[i2];
+  predictor_vjp<D>(W, dMh, dti, Mpa, in_a);
   for (int dd = 0; dd < D; ++dd) {
     const double hm = fg.hfp[dd][ec[dd]];
     for (int v = 0; v < V; ++v) in_a[V + dd * V + v] += Sa[dd][v] * 0.5 * hm;

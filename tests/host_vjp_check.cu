@@ -1,6 +1,7 @@
 // Host-side check of the reverse-mode vector-Jacobian products of the
 // pointwise Euler maps (spd_vjp.cuh) against products formed with the
-// dual-number forms of the same maps (spd_device.cuh): random states in 1D,
+// dual-number forms of the same maps (spd_device.cuh) and of the
+// MUSCL-Hancock half-step prediction: random states in 1D,
 // 2D and 3D, every Riemann solver, conservative and primitive inputs, and
 // mirrored states (the velocity ties of reflective walls); and the
 // Markstein quotient div_rcp against IEEE division, bit for bit.  Exit
@@ -11,7 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
-#include "spd_vjp.cuh"
+#include "spd_adjoint.cuh"
 using namespace spd;
 
 template <int D>
@@ -105,6 +106,46 @@ long long check_div_rcp(std::mt19937_64& rng, long long n) {
   return bad;
 }
 
+// dual-number form of the MUSCL-Hancock half-step prediction (the forward's
+// k_muscl_cells arithmetic) and its Jacobian-transpose product
+template <int D>
+double check_predictor(std::mt19937_64& rng) {
+  constexpr int V = D + 2, P_ = D + 1, NT = V * (1 + D);
+  std::normal_distribution<double> N(0.0, 1.0);
+  std::uniform_real_distribution<double> Uu(0.5, 2.0);
+  double W[V], dMh[D][V], pra[V];
+  W[0] = Uu(rng);
+  W[P_] = Uu(rng);
+  for (int v = 1; v <= D; ++v) W[v] = N(rng);
+  for (int dd = 0; dd < D; ++dd)
+    for (int v = 0; v < V; ++v) dMh[dd][v] = N(rng);
+  for (int v = 0; v < V; ++v) pra[v] = N(rng);
+  const double dti = 0.01 + 0.1 * Uu(rng);
+  Dual<NT> w[V], dm[D][V], dtW[V];
+  for (int v = 0; v < V; ++v) { w[v] = Dual<NT>(W[v]); w[v].d[v] = 1.0; }
+  for (int dd = 0; dd < D; ++dd)
+    for (int v = 0; v < V; ++v) { dm[dd][v] = Dual<NT>(dMh[dd][v]); dm[dd][v].d[V + dd * V + v] = 1.0; }
+  for (int v = 0; v < V; ++v) dtW[v] = Dual<NT>(0.0);
+  for (int dd = 0; dd < D; ++dd) {
+    const int vel = dd + 1;
+    dtW[0] = dtW[0] - (w[vel] * dm[dd][0] + w[0] * dm[dd][vel]);
+    dtW[P_] = dtW[P_] - (w[vel] * dm[dd][P_] + 1.4 * w[P_] * dm[dd][vel]);
+    dtW[vel] = dtW[vel] - (w[vel] * dm[dd][vel] + dm[dd][P_] / w[0]);
+    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - w[vel] * dm[dd][v2];
+  }
+  dtW[P_] = dtW[P_] * 0.0;
+  double ref[NT], got[NT];
+  for (int i = 0; i < NT; ++i) { ref[i] = 0.0; got[i] = 0.0; }
+  for (int v = 0; v < V; ++v) {
+    const Dual<NT> pr = w[v] + 0.5 * dtW[v] * dti;
+    for (int i = 0; i < NT; ++i) ref[i] += pra[v] * pr.d[i];
+  }
+  predictor_vjp<D>(W, dMh, dti, pra, got);
+  double err = 0.0, nrm = 0.0;
+  for (int i = 0; i < NT; ++i) { err += (got[i] - ref[i]) * (got[i] - ref[i]); nrm += ref[i] * ref[i]; }
+  return sqrt(err / nrm);
+}
+
 int main() {
   std::mt19937_64 rng(42);
   double worst = 0.0;
@@ -121,6 +162,9 @@ int main() {
         for (int d = 0; d < 3; ++d) { e = check<3>(rng, solver, prims, d, ties); worst = e > worst ? e : worst; }
       }
     double e = check_flux_prim<2>(rng, trial % 2); worst = e > worst ? e : worst;
+    e = check_predictor<1>(rng); worst = e > worst ? e : worst;
+    e = check_predictor<2>(rng); worst = e > worst ? e : worst;
+    e = check_predictor<3>(rng); worst = e > worst ? e : worst;
     e = check_flux_prim<3>(rng, trial % 3); worst = e > worst ? e : worst;
     e = check_flux_prim<1>(rng, 0); worst = e > worst ? e : worst;
   }
