@@ -537,10 +537,10 @@ def adjoint_arm(args):
             "backward_top_kernels_ms": {k: [v[0], round(v[1], 3)] for k, v in top}}
     if args.fd_dirs:
         line["fd_check"] = adjoint_fd_check(s, U0, target, r.dts, g, args.fd_dirs)
+    s.close()
     if args.batch > 1:
         line["batch"] = adjoint_batch(args, make_batch=lambda i: make(seed=100 + i), n=n, nsteps=nsteps)
     print(json.dumps(line), flush=True)
-    s.close()
 
 
 def adjoint_fd_check(s, U0, target, dts, g, ndirs, eps=1e-6, seed=2028):
@@ -611,8 +611,12 @@ def adjoint_batch(args, make_batch, n, nsteps):
         targets.append(AdjointRunner(sm, nsteps).forward(Ut)[0].clone())
     torch.cuda.synchronize()
 
+    # a record slot holds ~1 GB at 256^2 against 34 MB per U_sp checkpoint:
+    # 16 concurrent instances keep 4 slots each (checkpoints every 4 steps)
+    every = 4
+
     def one(i):
-        r = AdjointRunner(sims[i], nsteps)
+        r = AdjointRunner(sims[i], nsteps, checkpoint_every=every)
         y = r.forward(U0s[i])
         res = y[0] - targets[i]
         gy = torch.zeros_like(y)
@@ -627,7 +631,8 @@ def adjoint_batch(args, make_batch, n, nsteps):
     wall = time.perf_counter() - t0
     for sm in sims:
         sm.close()
-    return {"instances": B, "wall_s": wall, "gradients_per_s": B / wall, "grad_rho_norms": norms}
+    return {"instances": B, "wall_s": wall, "gradients_per_s": B / wall, "checkpoint_every": every,
+            "grad_rho_norms": norms}
 
 
 def main():
