@@ -186,7 +186,8 @@ def fp64_peak_tflops():
 # CPU baseline: the oracle restatement of the reference's NumPy path
 # ---------------------------------------------------------------------------
 def _cpu_worker(args):
-    workload, n_side, steps, warmup = args
+    workload, n_side, steps, warmup = args[:4]
+    want_state = len(args) > 4 and args[4]
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     sys.path.insert(0, ROOT)
     import warnings
@@ -221,17 +222,39 @@ def _cpu_worker(args):
         o.perform_update()
     el = time.perf_counter() - t0
     dof, _ = dof_of(kw)
+    if want_state:
+        return dof * steps, el, np.asarray(o.U_sp)
     return dof * steps, el
 
 
-def cpu_baseline(workload, n_side, steps, warmup, procs):
+def cpu_baseline(workload, n_side, steps, warmup, procs, want_state=False):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_worker, [(workload, n_side, steps, warmup)] * procs)
+        res = pool.map(_cpu_worker, [(workload, n_side, steps, warmup, want_state)] * procs)
     total_units = sum(r[0] for r in res)
     tmax = max(r[1] for r in res)
+    if want_state:
+        return total_units / tmax, tmax, res[0][2]
     return total_units / tmax, tmax
+
+
+def sample_parity(workload, n_side, U_oracle):
+    """The same sample (n_side cells per direction, one step from the
+    initial state) on the GPU against the oracle's U_sp."""
+    import numpy as np
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(verbose=False, **workload_kwargs(workload, n_side))
+    s.compute_dt()
+    s.perform_update()
+    U = s.dm.U_sp
+    s.close()
+    dev = np.abs(U - U_oracle)
+    rel = dev / np.maximum(np.abs(U_oracle), 1e-300)
+    ndim = (U.ndim - 1) // 2
+    return {"sample": "x".join([str(n_side)] * ndim) + " cells, 1 step from the initial state",
+            "max_abs_dev": float(np.nanmax(dev)), "max_rel_dev": float(np.nanmax(rel)),
+            "bitwise_equal": bool(np.array_equal(U, U_oracle, equal_nan=True))}
 
 
 def reference_arm(args):
@@ -379,9 +402,11 @@ def ours(args):
     line = None
     if rank == 0:
         cpu = None
+        parity = None
         if world == 1 and not args.no_cpu_baseline:
             sample_n = 128 if len(kw["N"]) == 2 else 16
-            v, tmax = cpu_baseline(args.workload, sample_n, 1, 0, 1)
+            v, tmax, U_oracle = cpu_baseline(args.workload, sample_n, 1, 0, 1, want_state=True)
+            parity = sample_parity(args.workload, sample_n, U_oracle)
             cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                    "sample": f"1 step of the same configuration at {'x'.join([str(sample_n)] * len(kw['N']))} cells on one core "
                              "(CPU restatement of the reference's NumPy path)"}
@@ -396,7 +421,8 @@ def ours(args):
                                  f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
                 "roofline": roof,
                 "fp64_gemm_peak_tflops": fp64,
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+                "cpu_baseline": cpu, "parity_vs_oracle": parity, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clocks,
                 "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
                 "kernel_share_of_step": total_kernel_ms / ms if ms else None}
         print(json.dumps(line), flush=True)

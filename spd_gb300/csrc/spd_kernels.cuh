@@ -124,10 +124,13 @@ __global__ void k_traces_ader(Ops op, Geo g, const double* __restrict__ U, int T
 // element-interface Riemann fluxes for direction d
 // (src/sdader_simulator.py:225-234, src/sd_boundary.py:7-76)
 // ---------------------------------------------------------------------------
-template <int D, int P, int BM = 0>
-__global__ void k_riemann_sd(Geo g, int d, int Teff, int solver, const double* __restrict__ trace,
+// DIR >= 0 fixes the direction at compile time (the rotated velocity
+// indices become constants); DIR = -1 takes it from d_rt.
+template <int D, int P, int BM = 0, int DIR = -1>
+__global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
                              const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape = nullptr) {
   using k = K<D, P>;
+  const int d = (DIR >= 0) ? DIR : d_rt;
   const long long nI = n_iface(g, d);
   const long long total = (long long)Teff * k::NJ * nI;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -238,6 +241,7 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
   if (active) {
     int cx, cy, cz;
     cell_coords(g, c, cx, cy, cz);
+#pragma unroll
     for (int d = 0; d < D; ++d) {
       const long long nI = n_iface(g, d);
       const int cd = (d == 0) ? cx : (d == 1 ? cy : cz);

@@ -83,8 +83,16 @@ struct Stepper : StepperBase {
         {
           ProfScope ps_(C, "k_riemann_sd");
           if (C->tape_mode == 0) {
-            k_riemann_sd<D, P><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                            C->bcfix[d], C->Fi[d]);
+            const unsigned nb = blocks_for(tot, 128);
+            if (d == 0)
+              k_riemann_sd<D, P, 0, 0><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d], C->bcfix[d],
+                                                                  C->Fi[d]);
+            else if (d == 1)
+              k_riemann_sd<D, P, 0, (D > 1 ? 1 : 0)><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
+                                                                                C->bcfix[d], C->Fi[d]);
+            else
+              k_riemann_sd<D, P, 0, (D > 2 ? 2 : 0)><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
+                                                                                C->bcfix[d], C->Fi[d]);
           } else {
             unsigned* tp = C->tape_rs[d] + ((size_t)C->tape_step * C->T + it) * C->T * k::NJ * n_iface(g, d);
             if (C->tape_mode == 1)
