@@ -53,10 +53,11 @@ struct Stepper : StepperBase {
   using k = K<D, P>;
 
   int configure(spd_ctx* C) override {
-    // cells per block of the interior kernel: bounded by 200 KB of shared memory
+    // cells per block of the interior kernel: bounded by the 227 KB of shared
+    // memory a block may use
     const size_t per_cell = (size_t)k::V * k::NS * C->T * sizeof(double);
     max_cpb = 64;
-    while (max_cpb > 1 && per_cell * max_cpb > 200 * 1024) max_cpb /= 2;
+    while (max_cpb > 1 && per_cell * max_cpb > 227 * 1024) max_cpb /= 2;
     cpb = std::min(32, max_cpb);
     smem = per_cell * max_cpb;
     CK(cudaFuncSetAttribute(k_interior<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
