@@ -257,6 +257,23 @@ def sample_parity(workload, n_side, U_oracle):
             "bitwise_equal": bool(np.array_equal(U, U_oracle, equal_nan=True))}
 
 
+def vortex_t1_error():
+    """The vortex configuration (32x32 cells on [0,10]^2, p=3, LLF, FV with
+    limiting) run to t=1: L1 error of the subcell-averaged density against
+    the exact translated vortex."""
+    import numpy as np
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import isentropic_vortex
+    from spd_gb300.polynomials import quadrature_mean
+    s = SDADER_Simulator(verbose=False, **workload_kwargs("vortex32"))
+    s.perform_time_evolution(1.0)
+    exact = s.crop(quadrature_mean(s.mesh_cv, isentropic_vortex(center=(6.0, 6.0)), 2, 0, light=False)[None])[0]
+    err = float(np.mean(np.abs(s.dm.W_cv[0] - exact)))
+    out = {"t_end": 1.0, "steps": s.n_step, "l1_density_error_vs_exact": err}
+    s.close()
+    return out
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -421,7 +438,9 @@ def ours(args):
                                  f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
                 "roofline": roof,
                 "fp64_gemm_peak_tflops": fp64,
-                "cpu_baseline": cpu, "parity_vs_oracle": parity, "e2e": e2e, "gpu_launches": launches,
+                "cpu_baseline": cpu, "parity_vs_oracle": parity,
+                "vortex_t1": vortex_t1_error() if args.workload == "vortex32" else None,
+                "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks,
                 "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
                 "kernel_share_of_step": total_kernel_ms / ms if ms else None}
