@@ -166,6 +166,8 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   std::memcpy(C->ops.sp_to_cv, ops->sp_to_cv, sizeof(double) * n * n);
   std::memcpy(C->ops.invader, ops->invader, sizeof(double) * T * T);
   std::memcpy(C->ops.w_tp, ops->w_tp, sizeof(double) * T);
+  for (int d = 0; d < 3; ++d)
+    for (int i = 0; i < n * nf; ++i) C->ops.dfp_h[d][i] = C->ops.dfp_to_sp[i] * g.inv_h[d];
 
   CK(cudaStreamCreateWithFlags(&C->own_stream, cudaStreamNonBlocking));
   C->stream = C->own_stream;

@@ -22,6 +22,10 @@ struct Ops {
   double sp_to_cv[MAXN * MAXN];
   double invader[MAXT * MAXT];
   double w_tp[MAXT];
+  // dfp_to_sp * (1/h_d) for directions whose h_d is a power of two: scaling
+  // every product and partial sum of the derivative by 2^k is exact (away
+  // from underflow and overflow), so sum(dfp*F)*(1/h) == sum((dfp/h)*F)
+  double dfp_h[3][MAXN * MAXNF];
 };
 
 struct Geo {
@@ -283,8 +287,8 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
           for (int v = 0; v < k::V; ++v) {
 #pragma unroll
             for (int so = 0; so < k::n; ++so) {
-              const double dsum = dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d);
-              const double val = pow2 ? dsum * ihd : div_rcp(dsum, hd, ihd);
+              const double val = pow2 ? dot_dir<k::nf>(op.dfp_h[d] + so * k::nf, Fl[v], d)
+                                      : div_rcp(dot_dir<k::nf>(op.dfp_to_sp + so * k::nf, Fl[v], d), hd, ihd);
               const int s = sp_index<D, P>(d, j, so);
               double* slot = &dudt_s[(((long long)v * k::NS + s) * Teff + tl) * CPB + cl];
               *slot = (d == 0) ? val : *slot + val;
