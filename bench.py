@@ -363,6 +363,17 @@ def ours(args):
     clocks = clk.summary()
     value = whole_job_rate(dof, args.steps, world, ms)
 
+    # the same steps through perform_iterations' driver: one captured step
+    # (CUDA graph) replayed per step, dt and time kept on the device
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    s.time, _, _ = ctx.step(args.steps, 0.0, 0, s.time)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1)
+    graph_driver = {"ms_per_step": graph_ms / args.steps, "value": whole_job_rate(dof, args.steps, 1, graph_ms)}
+
     # end to end through the public API with host buffers
     shape_u = s._shape_of("U_sp")
     shape_w = s._shape_of("W_cv")
@@ -440,6 +451,7 @@ def ours(args):
                 "fp64_gemm_peak_tflops": fp64,
                 "cpu_baseline": cpu, "parity_vs_oracle": parity,
                 "vortex_t1": vortex_t1_error() if args.workload == "vortex32" else None,
+                "graph_driver": graph_driver,
                 "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks,
                 "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},

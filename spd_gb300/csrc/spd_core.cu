@@ -43,6 +43,8 @@ __global__ void k_sd_layout(Geo g, int D, int n, int V, const double* __restrict
   else dst[r] = src[di];
 }
 
+__global__ void k_time_add_dev(double* t, const double* dt) { *t = *t + *dt; }
+
 StepperBase* make_stepper(int D, int P) {
   switch (D) {
     case 1: return make_stepper_d1(P);
@@ -297,6 +299,8 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
 int spd_destroy(spd_ctx* C) {
   if (!C) return SPD_ERR_ARG;
   if (C->stream) cudaStreamSynchronize(C->stream);
+  if (C->step_exec) cudaGraphExecDestroy(C->step_exec);
+  if (C->step_graph) cudaGraphDestroy(C->step_graph);
   for (void* p : C->allocs) cudaFree(p);
   for (void* p : C->adj_allocs) cudaFree(p);
   for (void* p : C->tape_allocs) cudaFree(p);
@@ -537,11 +541,76 @@ int spd_perform_update(spd_ctx* C, double* time_inout) {
   return SPD_OK;
 }
 
+// Capture one step (cmax, update, t_dev += dt) into the context's graph.
+// Returns false (and leaves the context as it was) when capture is not
+// possible; the caller then steps launch by launch.
+static bool build_step_graph(spd_ctx* C) {
+  if (C->step_exec) return true;
+  if (C->step_graph_failed) return false;
+  if (!C->t_dev) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(double)) != cudaSuccess) {
+      C->step_graph_failed = true;
+      return false;
+    }
+    C->allocs.push_back(p);
+    C->t_dev = static_cast<double*>(p);
+  }
+  double* keep_cv = C->U_cv;
+  double* keep_new = C->U_new;
+  double* keep_theta = C->theta_final;
+  cudaStream_t s = C->stream;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    C->step_graph_failed = true;
+    return false;
+  }
+  const long long launches = C->launches;
+  int rc = C->stepper->cmax(C);
+  if (!rc) rc = C->stepper->update(C);
+  if (!rc) {
+    k_time_add_dev<<<1, 1, 0, s>>>(C->t_dev, C->dt);
+    if (cudaGetLastError() != cudaSuccess) rc = SPD_ERR_CUDA;
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(s, &g);
+  C->graph_kernels = C->launches - launches + 1;  // the step's kernels and the time add
+  C->launches = launches;                          // capture launched nothing
+  C->graph_U_cv = C->U_cv;
+  C->graph_U_new = C->U_new;
+  C->graph_theta = C->theta_final;
+  if (rc || ec != cudaSuccess || cudaGraphInstantiate(&C->step_exec, g, 0) != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    C->step_exec = nullptr;
+    C->U_cv = keep_cv;
+    C->U_new = keep_new;
+    C->theta_final = keep_theta;
+    C->step_graph_failed = true;
+    cudaGetLastError();
+    return false;
+  }
+  C->step_graph = g;
+  return true;
+}
+
 int spd_step(spd_ctx* C, int nsteps, double t_end, int mode, double* time_inout, int* nsteps_done) {
   if (!C || !time_inout) return SPD_ERR_ARG;
   int done = 0;
   bool nonfinite = false;
-  if (mode == 0) {
+  if (mode == 0 && nsteps > 0 && !C->prof && C->tape_mode == 0 && !C->recording && build_step_graph(C)) {
+    // every step in one graph launch, time accumulated on the device in the
+    // same double additions as the host loop
+    CK(cudaMemcpyAsync(C->t_dev, time_inout, sizeof(double), cudaMemcpyHostToDevice, C->stream));
+    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(C->step_exec, C->stream));
+    C->launches += (long long)nsteps * C->graph_kernels;
+    CK(cudaMemcpyAsync(time_inout, C->t_dev, sizeof(double), cudaMemcpyDeviceToHost, C->stream));
+    CK(cudaStreamSynchronize(C->stream));
+    C->U_cv = C->graph_U_cv;
+    C->U_new = C->graph_U_new;
+    C->theta_final = C->graph_theta;
+    if (C->cfg.update == SPD_UPDATE_FV && C->cfg.FB) C->fb_ran = true;
+    done = nsteps;
+    nonfinite = !std::isfinite(*time_inout);
+  } else if (mode == 0) {
     for (int i = 0; i < nsteps; ++i) {
       if (int r = C->stepper->cmax(C)) return r;
       if (int r = spd_perform_update(C, time_inout)) return r;

@@ -31,7 +31,15 @@ struct spd_ctx {
   // state
   double *U_sp = nullptr, *U_cv = nullptr, *W_cv = nullptr, *U_new = nullptr;
   double* dt = nullptr;
-  double* t_dev = nullptr;  // simulated time kept on the device by the ensemble driver
+  double* t_dev = nullptr;  // simulated time kept on the device (ensemble driver, step graph)
+  // one captured step (CFL dt, update, time += dt) replayed by spd_step
+  // mode 0; the host-side buffer roles it leaves behind are restored after
+  // each replay
+  cudaGraph_t step_graph = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  bool step_graph_failed = false;
+  double *graph_U_cv = nullptr, *graph_U_new = nullptr, *graph_theta = nullptr;
+  long long graph_kernels = 0;
   // adjoint: record slots of forward intermediates and the adjoint work
   // arrays (allocated by spd_adjoint_enable, freed on re-enable and destroy)
   bool recording = false;

@@ -14,6 +14,9 @@ using namespace spd_host;
 
 struct spd_ensemble {
   std::vector<spd_ctx*> ctx;
+  // buffer roles of each context at the end of the captured steps (the graph
+  // replays leave the data there)
+  std::vector<double*> roles;
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> join;
   cudaStream_t main = nullptr;
@@ -117,6 +120,11 @@ int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launc
   if (ec != cudaSuccess) return efail(E, SPD_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ec));
   E->graph = g;
   ECK(cudaGraphInstantiate(&E->exec, E->graph, 0));
+  for (spd_ctx* C : E->ctx) {
+    E->roles.push_back(C->U_cv);
+    E->roles.push_back(C->U_new);
+    E->roles.push_back(C->theta_final);
+  }
   *out = holder.release();
   return SPD_OK;
 }
@@ -124,6 +132,11 @@ int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launc
 int spd_ensemble_step(spd_ensemble* E, int nlaunch) {
   if (!E || nlaunch < 0) return SPD_ERR_ARG;
   for (int i = 0; i < nlaunch; ++i) ECK(cudaGraphLaunch(E->exec, E->main));
+  for (size_t i = 0; i < E->ctx.size(); ++i) {
+    E->ctx[i]->U_cv = E->roles[3 * i];
+    E->ctx[i]->U_new = E->roles[3 * i + 1];
+    E->ctx[i]->theta_final = E->roles[3 * i + 2];
+  }
   return SPD_OK;
 }
 
@@ -164,6 +177,14 @@ const char* spd_ensemble_last_error(const spd_ensemble* E) { return E ? E->err.c
 
 int spd_set_cells_per_block(spd_ctx* C, int cpb) {
   if (!C || cpb < 1 || cpb > C->stepper->max_cpb || (cpb & (cpb - 1))) return SPD_ERR_ARG;
+  if (C->stepper->cpb != cpb && C->step_exec) {
+    // the captured step carries the old launch shape
+    cudaStreamSynchronize(C->stream);
+    cudaGraphExecDestroy(C->step_exec);
+    cudaGraphDestroy(C->step_graph);
+    C->step_exec = nullptr;
+    C->step_graph = nullptr;
+  }
   C->stepper->cpb = cpb;
   return SPD_OK;
 }

@@ -1,0 +1,58 @@
+"""perform_iterations replays one captured step (CUDA graph: CFL dt,
+update, device-side time accumulation); the result is the launch-by-launch
+loop's, bit for bit, also when graph replays and single steps are mixed and
+when the number of FV substeps is odd (buffer roles alternate)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _make(p):
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import four_quadrant
+    return SDADER_Simulator(p=p, N=(24, 24), init_fct=four_quadrant, update="FV", FB=True,
+                            riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                            BC=(("gradfree", "gradfree"),) * 2, verbose=False)
+
+
+def _loop(s, n):
+    for _ in range(n):
+        s.compute_dt()
+        s.perform_update()
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_graph_steps_equal_launch_by_launch(p):
+    a, b = _make(p), _make(p)
+    # perform_iterations ends with end_sim (U_cv, W_cv from U_sp), as in the
+    # reference; the launch-by-launch run does the same at the same points
+    _loop(a, 3)
+    a._ctx.end_sim()
+    _loop(a, 4)
+    a._ctx.end_sim()
+    b.perform_iterations(3)   # graph
+    _loop(b, 1)               # single step in between
+    b.perform_iterations(3)   # graph again
+    assert b.n_step == a.n_step == 7
+    assert b.time == a.time
+    for key in ("U_sp", "U_cv", "W_cv", "troubles", "theta"):
+        assert np.array_equal(getattr(a.dm, key), getattr(b.dm, key), equal_nan=True), key
+    a.close()
+    b.close()
+
+
+def test_graph_counts_its_kernel_launches():
+    s = _make(3)
+    s.perform_iterations(1)
+    n0 = s._ctx.launch_count()
+    s.perform_iterations(4)             # 4 graph steps + end_sim (2 kernels)
+    per_step = (s._ctx.launch_count() - n0 - 2) / 4
+    s._ctx.profile(True)                # profiling steps launch by launch
+    n1 = s._ctx.launch_count()
+    s.perform_iterations(1)
+    s._ctx.profile(False)
+    s._ctx.profile_report()
+    single = s._ctx.launch_count() - n1 - 2
+    assert per_step == single + 1       # + the device time add
+    s.close()
