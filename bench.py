@@ -416,9 +416,9 @@ def ours(args):
         achieved = per_launch_bytes / avg_s / 1e9
         # DRAM bytes (read + write) per k_interior launch from one ncu capture of
         # the 2D p=3 four-quadrant step at 256^2 (mean over the 4 launches of a
-        # step: 338, 473, 474, 594 MB; profiles/k_interior_quadrant256_p3.md),
+        # step: 329, 454, 454, 556 MB; profiles/k_interior_quadrant256_p3.md),
         # scaled by the cell count (traffic grows in proportion)
-        traffic = 469.811968e6 * cells / 65536 if (D, p) == (2, 3) else None
+        traffic = 448.170496e6 * cells / 65536 if (D, p) == (2, 3) else None
         roof = {"bound": "hbm", "kernel": "k_interior", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                 "frac": achieved / peak_gbs, "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3}
@@ -428,6 +428,20 @@ def ours(args):
             fp64 = fp64_peak_tflops()
         except Exception:
             fp64 = None
+    # The binding roof: the FP64 pipe.  k_interior executes 42,966 FP64
+    # instructions (DADD + DMUL + DFMA, thread level) per cell and step in
+    # 2D at p=3, whatever the data (ncu smsp__sass_thread_inst_executed_op_
+    # {dadd,dmul,dfma}_pred_on.sum over the 4 launches of a 256^2 step / 65,536
+    # cells; profiles/k_interior_quadrant256_p3.md).  The peak is the issue
+    # rate cuBLAS DGEMM reaches (one DFMA per 2 flops).
+    fp64_roof = None
+    if roof is not None and fp64 and (D, p) == (2, 3):
+        k_ms_step = prof["k_interior"][1] / args.steps
+        rate = 42966.0 * cells / (k_ms_step / 1e3)
+        peak = fp64 * 1e12 / 2.0
+        fp64_roof = {"bound": "fp64 pipe", "kernel": "k_interior", "achieved": rate / 1e9, "peak": peak / 1e9,
+                     "unit": "G FP64 instructions/s", "frac": rate / peak,
+                     "peak_kind": "measured (cuBLAS DGEMM issue rate)"}
     line = None
     if rank == 0:
         cpu = None
@@ -449,6 +463,7 @@ def ours(args):
                            "l2": "inputs larger than L2: U_sp alone is "
                                  f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
                 "roofline": roof,
+                "roofline_fp64": fp64_roof,
                 "fp64_gemm_peak_tflops": fp64,
                 "cpu_baseline": cpu, "parity_vs_oracle": parity,
                 "vortex_t1": vortex_t1_error() if args.workload == "vortex32" else None,
