@@ -430,12 +430,12 @@ def ours(args):
             fp64 = None
     # The binding roof: the FP64 pipe.  k_interior executes 42,966 FP64
     # instructions (DADD + DMUL + DFMA, thread level) per cell and step in
-    # 2D at p=3, whatever the data (ncu smsp__sass_thread_inst_executed_op_
+    # 2D at p=3 with the FV update, whatever the data (ncu smsp__sass_thread_inst_executed_op_
     # {dadd,dmul,dfma}_pred_on.sum over the 4 launches of a 256^2 step / 65,536
     # cells; profiles/k_interior_quadrant256_p3.md).  The peak is the issue
     # rate cuBLAS DGEMM reaches (one DFMA per 2 flops).
     fp64_roof = None
-    if roof is not None and fp64 and (D, p) == (2, 3):
+    if roof is not None and fp64 and (D, p) == (2, 3) and kw.get("update") == "FV":
         k_ms_step = prof["k_interior"][1] / args.steps
         rate = 42966.0 * cells / (k_ms_step / 1e3)
         peak = fp64 * 1e12 / 2.0
