@@ -44,6 +44,12 @@ __global__ void k_sd_layout(Geo g, int D, int n, int V, const double* __restrict
 }
 
 __global__ void k_time_add_dev(double* t, const double* dt) { *t = *t + *dt; }
+// perform_time_evolution's clip (src/sdader_simulator.py:406-409) on the
+// device: t[0] = time, t[1] = t_end
+__global__ void k_clip_dt(const double* t, double* dt) {
+  const double d = *dt;
+  if (t[0] + d >= t[1]) *dt = t[1] - t[0];
+}
 
 StepperBase* make_stepper(int D, int P) {
   switch (D) {
@@ -301,6 +307,8 @@ int spd_destroy(spd_ctx* C) {
   if (C->stream) cudaStreamSynchronize(C->stream);
   if (C->step_exec) cudaGraphExecDestroy(C->step_exec);
   if (C->step_graph) cudaGraphDestroy(C->step_graph);
+  if (C->dt_exec) cudaGraphExecDestroy(C->dt_exec);
+  if (C->dt_graph) cudaGraphDestroy(C->dt_graph);
   for (void* p : C->allocs) cudaFree(p);
   for (void* p : C->adj_allocs) cudaFree(p);
   for (void* p : C->tape_allocs) cudaFree(p);
@@ -541,54 +549,77 @@ int spd_perform_update(spd_ctx* C, double* time_inout) {
   return SPD_OK;
 }
 
-// Capture one step (cmax, update, t_dev += dt) into the context's graph.
+// Capture one step into two graphs: the dt graph (CFL reduction, then the
+// clip of perform_time_evolution: dt = t_end - t where t + dt >= t_end, with
+// t and t_end in t_dev[0..1]) and the update graph (update, t_dev[0] += dt).
 // Returns false (and leaves the context as it was) when capture is not
 // possible; the caller then steps launch by launch.
+static bool capture(spd_ctx* C, int part, cudaGraph_t* gout, cudaGraphExec_t* xout) {
+  cudaStream_t s = C->stream;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+  int rc;
+  if (part == 0) {
+    rc = C->stepper->cmax(C);
+    if (!rc) {
+      k_clip_dt<<<1, 1, 0, s>>>(C->t_dev, C->dt);
+      if (cudaGetLastError() != cudaSuccess) rc = SPD_ERR_CUDA;
+    }
+  } else {
+    rc = C->stepper->update(C);
+    if (!rc) {
+      k_time_add_dev<<<1, 1, 0, s>>>(C->t_dev, C->dt);
+      if (cudaGetLastError() != cudaSuccess) rc = SPD_ERR_CUDA;
+    }
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(s, &g);
+  if (rc || ec != cudaSuccess || cudaGraphInstantiate(xout, g, 0) != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    *xout = nullptr;
+    cudaGetLastError();
+    return false;
+  }
+  *gout = g;
+  return true;
+}
+
 static bool build_step_graph(spd_ctx* C) {
   if (C->step_exec) return true;
   if (C->step_graph_failed) return false;
-  if (!C->t_dev) {
+  if (!C->t_dev_pair) {
     void* p = nullptr;
-    if (cudaMalloc(&p, sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&p, 2 * sizeof(double)) != cudaSuccess) {
       C->step_graph_failed = true;
       return false;
     }
     C->allocs.push_back(p);
-    C->t_dev = static_cast<double*>(p);
+    C->t_dev_pair = static_cast<double*>(p);
   }
+  double* keep_t = C->t_dev;
+  C->t_dev = C->t_dev_pair;
   double* keep_cv = C->U_cv;
   double* keep_new = C->U_new;
   double* keep_theta = C->theta_final;
-  cudaStream_t s = C->stream;
-  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-    C->step_graph_failed = true;
-    return false;
-  }
   const long long launches = C->launches;
-  int rc = C->stepper->cmax(C);
-  if (!rc) rc = C->stepper->update(C);
-  if (!rc) {
-    k_time_add_dev<<<1, 1, 0, s>>>(C->t_dev, C->dt);
-    if (cudaGetLastError() != cudaSuccess) rc = SPD_ERR_CUDA;
-  }
-  cudaGraph_t g = nullptr;
-  const cudaError_t ec = cudaStreamEndCapture(s, &g);
-  C->graph_kernels = C->launches - launches + 1;  // the step's kernels and the time add
+  const bool ok = capture(C, 0, &C->dt_graph, &C->dt_exec) && capture(C, 1, &C->step_graph, &C->step_exec);
+  C->graph_kernels = C->launches - launches + 2;  // the step's kernels, the clip and the time add
   C->launches = launches;                          // capture launched nothing
   C->graph_U_cv = C->U_cv;
   C->graph_U_new = C->U_new;
   C->graph_theta = C->theta_final;
-  if (rc || ec != cudaSuccess || cudaGraphInstantiate(&C->step_exec, g, 0) != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
+  C->t_dev = keep_t;
+  if (!ok) {
+    if (C->dt_exec) cudaGraphExecDestroy(C->dt_exec);
+    if (C->dt_graph) cudaGraphDestroy(C->dt_graph);
+    C->dt_exec = nullptr;
+    C->dt_graph = nullptr;
     C->step_exec = nullptr;
     C->U_cv = keep_cv;
     C->U_new = keep_new;
     C->theta_final = keep_theta;
     C->step_graph_failed = true;
-    cudaGetLastError();
     return false;
   }
-  C->step_graph = g;
   return true;
 }
 
@@ -596,20 +627,44 @@ int spd_step(spd_ctx* C, int nsteps, double t_end, int mode, double* time_inout,
   if (!C || !time_inout) return SPD_ERR_ARG;
   int done = 0;
   bool nonfinite = false;
-  if (mode == 0 && nsteps > 0 && !C->prof && C->tape_mode == 0 && !C->recording && build_step_graph(C)) {
-    // every step in one graph launch, time accumulated on the device in the
-    // same double additions as the host loop
-    CK(cudaMemcpyAsync(C->t_dev, time_inout, sizeof(double), cudaMemcpyHostToDevice, C->stream));
-    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(C->step_exec, C->stream));
-    C->launches += (long long)nsteps * C->graph_kernels;
-    CK(cudaMemcpyAsync(time_inout, C->t_dev, sizeof(double), cudaMemcpyDeviceToHost, C->stream));
+  const bool graphs = !C->prof && C->tape_mode == 0 && !C->recording && build_step_graph(C);
+  if (graphs) {
+    // the step as two graph launches; time and the clip in the same double
+    // operations as the host loop below
+    const double te = (mode == 0) ? HUGE_VAL : t_end;
+    const double tt[2] = {*time_inout, te};
+    CK(cudaMemcpyAsync(C->t_dev_pair, tt, sizeof(tt), cudaMemcpyHostToDevice, C->stream));
+    if (mode == 0) {
+      for (int i = 0; i < nsteps; ++i) {
+        CK(cudaGraphLaunch(C->dt_exec, C->stream));
+        CK(cudaGraphLaunch(C->step_exec, C->stream));
+      }
+      done = nsteps > 0 ? nsteps : 0;
+    } else {
+      double t = *time_inout;
+      while (t < t_end) {
+        CK(cudaGraphLaunch(C->dt_exec, C->stream));
+        double dt = 0.0;
+        CK(cudaMemcpyAsync(&dt, C->dt, sizeof(double), cudaMemcpyDeviceToHost, C->stream));
+        CK(cudaStreamSynchronize(C->stream));
+        if (dt < 1e-14) break;
+        CK(cudaGraphLaunch(C->step_exec, C->stream));
+        t = t + dt;
+        nonfinite = nonfinite || !std::isfinite(dt);
+        ++done;
+        if (nsteps > 0 && done >= nsteps) break;
+      }
+    }
+    C->launches += (long long)done * C->graph_kernels;
+    CK(cudaMemcpyAsync(time_inout, C->t_dev_pair, sizeof(double), cudaMemcpyDeviceToHost, C->stream));
     CK(cudaStreamSynchronize(C->stream));
-    C->U_cv = C->graph_U_cv;
-    C->U_new = C->graph_U_new;
-    C->theta_final = C->graph_theta;
-    if (C->cfg.update == SPD_UPDATE_FV && C->cfg.FB) C->fb_ran = true;
-    done = nsteps;
-    nonfinite = !std::isfinite(*time_inout);
+    if (done) {
+      C->U_cv = C->graph_U_cv;
+      C->U_new = C->graph_U_new;
+      C->theta_final = C->graph_theta;
+      if (C->cfg.update == SPD_UPDATE_FV && C->cfg.FB) C->fb_ran = true;
+    }
+    nonfinite = nonfinite || !std::isfinite(*time_inout);
   } else if (mode == 0) {
     for (int i = 0; i < nsteps; ++i) {
       if (int r = C->stepper->cmax(C)) return r;

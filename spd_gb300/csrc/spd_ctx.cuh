@@ -32,11 +32,12 @@ struct spd_ctx {
   double *U_sp = nullptr, *U_cv = nullptr, *W_cv = nullptr, *U_new = nullptr;
   double* dt = nullptr;
   double* t_dev = nullptr;  // simulated time kept on the device (ensemble driver, step graph)
-  // one captured step (CFL dt, update, time += dt) replayed by spd_step
-  // mode 0; the host-side buffer roles it leaves behind are restored after
-  // each replay
-  cudaGraph_t step_graph = nullptr;
-  cudaGraphExec_t step_exec = nullptr;
+  // one captured step (dt graph: CFL dt and the t_end clip; update graph:
+  // update and time += dt) replayed by spd_step; the host-side buffer roles
+  // it leaves behind are restored after each replay
+  cudaGraph_t step_graph = nullptr, dt_graph = nullptr;
+  cudaGraphExec_t step_exec = nullptr, dt_exec = nullptr;
+  double* t_dev_pair = nullptr;  // [time, t_end] of the step graphs
   bool step_graph_failed = false;
   double *graph_U_cv = nullptr, *graph_U_new = nullptr, *graph_theta = nullptr;
   long long graph_kernels = 0;

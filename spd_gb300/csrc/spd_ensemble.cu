@@ -182,8 +182,12 @@ int spd_set_cells_per_block(spd_ctx* C, int cpb) {
     cudaStreamSynchronize(C->stream);
     cudaGraphExecDestroy(C->step_exec);
     cudaGraphDestroy(C->step_graph);
+    cudaGraphExecDestroy(C->dt_exec);
+    cudaGraphDestroy(C->dt_graph);
     C->step_exec = nullptr;
     C->step_graph = nullptr;
+    C->dt_exec = nullptr;
+    C->dt_graph = nullptr;
   }
   C->stepper->cpb = cpb;
   return SPD_OK;

@@ -1,7 +1,8 @@
-"""perform_iterations replays one captured step (CUDA graph: CFL dt,
-update, device-side time accumulation); the result is the launch-by-launch
-loop's, bit for bit, also when graph replays and single steps are mixed and
-when the number of FV substeps is odd (buffer roles alternate)."""
+"""perform_iterations and perform_time_evolution replay one captured step
+(CUDA graphs: CFL dt with the t_end clip; update with device-side time
+accumulation); the result is the launch-by-launch loop's, bit for bit, also
+when graph replays and single steps are mixed and when the number of FV
+substeps is odd (buffer roles alternate)."""
 import numpy as np
 import pytest
 
@@ -54,5 +55,23 @@ def test_graph_counts_its_kernel_launches():
     s._ctx.profile(False)
     s._ctx.profile_report()
     single = s._ctx.launch_count() - n1 - 2
-    assert per_step == single + 1       # + the device time add
+    assert per_step == single + 2       # + the device dt clip and time add
     s.close()
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_time_evolution_graph_equals_host_loop(p):
+    """perform_time_evolution replays the dt graph (with the t_end clip on
+    the device) and the update graph; profiling forces the host loop."""
+    a, b = _make(p), _make(p)
+    a._ctx.profile(True)
+    a.perform_time_evolution(0.02)
+    a._ctx.profile(False)
+    a._ctx.profile_report()
+    b.perform_time_evolution(0.02)
+    assert a.n_step == b.n_step > 1
+    assert a.time == b.time == 0.02
+    for key in ("U_sp", "U_cv", "W_cv", "troubles", "theta"):
+        assert np.array_equal(getattr(a.dm, key), getattr(b.dm, key), equal_nan=True), key
+    a.close()
+    b.close()
