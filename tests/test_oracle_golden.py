@@ -29,3 +29,18 @@ def test_oracle_sees_troubles():
     data, kw, meta = load("quadrant16_p3_fvfb_hllc_gradfree")
     assert data["troubles"].sum() > 0
     assert data["theta"].max() > 1.0  # boundary contamination of theta
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_torch_transcription_matches_reference_bitwise(name):
+    """The oracle run on torch tensors (the FP64 torch transcription whose
+    autograd gradient checks the CUDA adjoint) reproduces the reference's
+    outputs bit for bit, like the NumPy run."""
+    torch = pytest.importorskip("torch")
+    data, kw, meta = load(name)
+    o = oracle_from_golden({**data, "init_U_sp": torch.tensor(data["init_U_sp"])}, kw)
+    for _ in range(meta["steps"]):
+        o.compute_dt()
+        o.perform_update()
+    assert isinstance(o.U_sp, torch.Tensor)
+    assert np.array_equal(o.U_sp.numpy(), data["U_sp"])
