@@ -185,6 +185,20 @@ const char* spd_version(void);
  * steps.  The contexts stay owned by the caller and must outlive the
  * ensemble; their simulated time restarts at 0 in the device accumulator. */
 int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launch, spd_ensemble** out);
+/* Packed form of the same ensemble: every kernel launch of the step covers
+ * all instances at once.  A per-instance table of block offsets maps each
+ * thread block to its instance (geometry, buffers, its own dt) and to its
+ * block within that instance, so each instance computes exactly what its own
+ * step computes (bit-identical) while a whole ensemble step costs ~100
+ * launches instead of ~100 per instance; the sequence is captured in one
+ * CUDA graph.  The instances must share the dimension, degree, options and
+ * cells per block (they may differ in grid size, domain and boundary
+ * conditions); otherwise SPD_ERR_ARG with the reason in
+ * spd_ensemble_last_error(NULL). */
+int spd_ensemble_create_packed(spd_ctx** ctxs, int n, int steps_per_launch, spd_ensemble** out);
+/* Number of nodes (kernel launches, zero-fills, stream joins) of the
+ * ensemble's CUDA graph. */
+int spd_ensemble_graph_nodes(const spd_ensemble* ens, long long* nodes);
 /* Enqueue nlaunch graph launches (asynchronous). */
 int spd_ensemble_step(spd_ensemble* ens, int nlaunch);
 int spd_ensemble_synchronize(spd_ensemble* ens);
@@ -192,6 +206,8 @@ int spd_ensemble_synchronize(spd_ensemble* ens);
 int spd_ensemble_time(spd_ensemble* ens, int i, double* t_out);
 int spd_ensemble_set_time(spd_ensemble* ens, int i, double t);
 int spd_ensemble_destroy(spd_ensemble* ens);
+/* Last error of ``ens``; with NULL, the calling thread's most recent
+ * ensemble error (e.g. why a create failed). */
 const char* spd_ensemble_last_error(const spd_ensemble* ens);
 /* Cells per thread block of the predictor's fused interior kernel (a power
  * of two up to the shared-memory bound reported by the getter); a tuning

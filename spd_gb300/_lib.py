@@ -31,7 +31,8 @@ EXPORTS = (
     "spd_get_dt", "spd_perform_update", "spd_step", "spd_end_sim",
     "spd_synchronize", "spd_destroy", "spd_last_error", "spd_version",
     "spd_set_stream", "spd_profile", "spd_profile_report", "spd_launch_count",
-    "spd_cfl_dt_noalloc", "spd_ensemble_create", "spd_ensemble_step",
+    "spd_cfl_dt_noalloc", "spd_ensemble_create", "spd_ensemble_create_packed", "spd_ensemble_graph_nodes",
+    "spd_ensemble_step",
     "spd_ensemble_synchronize", "spd_ensemble_time", "spd_ensemble_set_time", "spd_ensemble_destroy", "spd_ensemble_last_error",
     "spd_set_cells_per_block", "spd_get_cells_per_block",
     "spd_adjoint_enable", "spd_adjoint_depth", "spd_record_step", "spd_vjp_step",

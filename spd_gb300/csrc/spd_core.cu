@@ -251,7 +251,7 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   if (int r = dalloc(C, &C->W_cv, (size_t)V * Nq)) return r;
   if (int r = dalloc(C, &C->dt, 1)) return r;
   if (int r = dalloc(C, &C->flags, 4)) return r;
-  if (int r = dalloc(C, &C->counts, 4)) return r;
+  if (int r = dalloc(C, &C->counts, 8)) return r;
   for (int d = 0; d < D; ++d) {
     const long long nI = Nc / g.N[d] * (g.N[d] + 1);
     if (int r = dalloc(C, &C->trace[d], (size_t)2 * V * T * NJ * Nc)) return r;
@@ -274,11 +274,13 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
       if (int r = dalloc(C, &C->theta_src, (size_t)Nqe)) return r;
       if (int r = dalloc(C, &C->theta_a, (size_t)Nqe)) return r;
       if (int r = dalloc(C, &C->theta_b, (size_t)Nqe)) return r;
-      if (int r = dalloc(C, &C->mask, (size_t)Nq)) return r;
+      // whole 32-bit words: k_sed clears mask bits with a word-wide atomic AND
+      if (int r = dalloc(C, &C->mask, (size_t)(Nq + 3) / 4 * 4)) return r;
       if (int r = dalloc(C, &C->mark_cell, (size_t)Nqe)) return r;
       if (int r = dalloc(C, &C->mark_q, (size_t)Nq)) return r;
       if (int r = dalloc(C, &C->list_cell, (size_t)Nqe)) return r;
       if (int r = dalloc(C, &C->list_q, (size_t)Nq)) return r;
+      if (int r = dalloc(C, &C->list_sed, (size_t)2 * Nq)) return r;
       if (int r = dalloc(C, &C->troubles, (size_t)Nq)) return r;
       if (int r = dalloc(C, &C->Mpred, (size_t)V * Nqe)) return r;
       if (int r = dalloc(C, &C->S, (size_t)D * V * Nqe)) return r;
@@ -291,6 +293,7 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
         const long long nfc = n_faces_host(g, d);
         if (int r = dalloc(C, &C->aff[d], (size_t)nfc)) return r;
         if (int r = dalloc(C, &C->F_FB[d], (size_t)V * nfc)) return r;
+        if (int r = dalloc(C, &C->list_face[d], (size_t)nfc)) return r;
         CK(cudaMemset(C->aff[d], 0, sizeof(double) * nfc));
       }
     }

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/spd_gb300.h"
+#include "spd_batch.cuh"
 #include "spd_fv.cuh"
 
 namespace spd_host {
@@ -90,8 +91,13 @@ struct spd_ctx {
   double* bcbuf[3] = {nullptr, nullptr, nullptr};
   unsigned char *mask = nullptr, *mark_cell = nullptr, *mark_q = nullptr;
   int* flags = nullptr;  // [0] any possible trouble, [1] nan in cmax, [2] marked faces
-  unsigned long long* counts = nullptr;  // [0] cells, [1] subcells, [2] cmax bits
-  long long *list_cell = nullptr, *list_q = nullptr;
+  // [0] marked extended cells, [1] marked subcells, [2] cmax bits, [3] subcells
+  // with a NAD flag on density or pressure, [4 + d] affected faces of direction d
+  unsigned long long* counts = nullptr;
+  // compacted index lists: marked extended cells, marked subcells, subcells
+  // needing the smoothness check, affected faces per direction
+  long long *list_cell = nullptr, *list_q = nullptr, *list_sed = nullptr;
+  long long* list_face[3] = {nullptr, nullptr, nullptr};
   double* troubles = nullptr;
   double* aff[3] = {nullptr, nullptr, nullptr};
   double* F_FB[3] = {nullptr, nullptr, nullptr};
@@ -102,6 +108,9 @@ struct spd_ctx {
   size_t staging_len = 0;
   spd_host::StepperBase* stepper = nullptr;
   bool fb_ran = false;
+  // while non-null, the step's launches and zero-fills are recorded into
+  // this batch recorder instead of being issued (packed ensembles)
+  spd_batch::BatchRec* brec = nullptr;
   // stream and launch accounting
   cudaStream_t own_stream = nullptr;
   long long launches = 0;
@@ -136,6 +145,28 @@ inline int fail(spd_ctx* c, int code, const std::string& msg) {
   } while (0)
 
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// Launch of the step kernel ``kern`` whose body is ``Body`` on the context's
+// stream, or, while a batch recorder is attached, the record of that launch
+// (its grid, block shape and argument pack) for a batched launch.
+template <class Body, class... P, class... A>
+void launch(spd_ctx* C, const char* name, void (*kern)(P...), dim3 grid, dim3 block, size_t smem, A&&... a) {
+  if (C->brec) {
+    C->brec->add<Body>(name, grid, block, smem, spd_batch::PackBuild<P...>::make(std::forward<A>(a)...));
+    return;
+  }
+  kern<<<grid, block, smem, C->stream>>>(std::forward<A>(a)...);
+}
+
+// zero-fill of device bytes on the context's stream (recorded while a batch
+// recorder is attached)
+inline cudaError_t zero_fill(spd_ctx* C, void* p, size_t bytes) {
+  if (C->brec) {
+    C->brec->add_zero(p, bytes);
+    return cudaSuccess;
+  }
+  return cudaMemsetAsync(p, 0, bytes, C->stream);
+}
 
 inline cudaEvent_t get_event(spd_ctx* C) {
   if (!C->pool.empty()) {

@@ -22,6 +22,17 @@ constexpr int MAXNF = 6;
 constexpr int MAXT = 6;   // m <= 5
 constexpr int NGH = 2;    // subcell ghost layers (Nghc)
 
+// Block index a kernel body works on and the number of blocks of its grid.
+// A plain launch passes the hardware indices; a batched launch over many
+// instances passes the block's index within its own instance's share of the
+// grid and the size of that share.
+struct Blk {
+  unsigned id, n;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ Blk hw_blk() { return Blk{blockIdx.x, gridDim.x}; }
+#endif
+
 enum Riemann : int { RS_LLF = 0, RS_HLLC = 1, RS_LHLLC = 2 };
 enum Limiter : int { LIM_MINMOD = 0, LIM_MONCEN = 1 };
 enum BcKind : int { BC_PERIODIC = 0, BC_REFLECTIVE = 1, BC_GRADFREE = 2, BC_IC = 3, BC_EQ = 4, BC_PRESSURE = 5 };
@@ -365,7 +376,26 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
     Pstar = div_by(rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR), den, rden);
   }
   S r, vg, Pg, e;
-  if (pick(br, sL > 0.0)) {
+  if constexpr (BM == 0) {
+    // the left and right star states are the same formulas with the sides
+    // swapped: one path with per-lane operands, so a warp whose lanes take
+    // both sides (an FP64 warp instruction costs the same with any number of
+    // active lanes) evaluates the reciprocal and quotients once
+    if (sL > 0.0) {
+      r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
+    } else if (vstar > 0.0 || sR > 0.0) {
+      const bool lft = vstar > 0.0;
+      const S s = lft ? sL : sR, v = lft ? vL : vR;
+      const S w0 = lft ? WL[0] : WR[0], wP = lft ? WL[P_] : WR[P_], uP = lft ? UL[P_] : UR[P_];
+      const S d = s - vstar;
+      const S rd = recip_of(d);
+      r = div_by(w0 * (s - v), d, rd);
+      e = div_by((s - v) * uP - wP * v + Pstar * vstar, d, rd);
+      vg = vstar; Pg = Pstar;
+    } else {
+      r = WR[0]; vg = vR; Pg = WR[P_]; e = UR[P_];
+    }
+  } else if (pick(br, sL > 0.0)) {
     r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
   } else if (pick(br, vstar > 0.0)) {
     const S d = sL - vstar;

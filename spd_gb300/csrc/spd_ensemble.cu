@@ -5,6 +5,11 @@
 // instances fill the GPU concurrently and a whole ensemble step costs one
 // graph launch instead of ~100 kernel launches and a host round trip per
 // instance.  Each instance keeps its own dt (its own device reduction).
+//
+// The packed form (spd_ensemble_create_packed) instead merges the i-th
+// launch of every instance into one batched launch indexed by a per-instance
+// block-offset table (spd_batch.cuh): a whole ensemble step is then ~100
+// launches however many instances there are.
 #include <memory>
 
 #include "spd_ctx.cuh"
@@ -24,15 +29,28 @@ struct spd_ensemble {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int steps_per_launch = 1;
+  // packed form: the batched launch sites (argument packs and block-offset
+  // tables in device memory) replayed by the graph
+  std::unique_ptr<spd_batch::BatchRec> packed;
   std::string err;
 };
 
 namespace {
 
-__global__ void k_time_add(double* t, const double* dt) { *t = *t + *dt; }
+struct TimeAdd {
+  static __device__ __forceinline__ void run(Blk, double* t, const double* dt) {
+    if (threadIdx.x == 0) *t = *t + *dt;
+  }
+};
+__global__ void k_time_add(double* t, const double* dt) { TimeAdd::run(hw_blk(), t, dt); }
+
+// the calling thread's most recent ensemble error (also of a failed create,
+// whose ensemble no longer exists)
+thread_local std::string t_last_err;
 
 int efail(spd_ensemble* E, int code, const std::string& msg) {
   if (E) E->err = msg;
+  t_last_err = msg;
   return code;
 }
 
@@ -129,6 +147,80 @@ int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launc
   return SPD_OK;
 }
 
+int spd_ensemble_create_packed(spd_ctx** ctxs, int n, int steps_per_launch, spd_ensemble** out) {
+  if (!ctxs || n <= 0 || steps_per_launch <= 0 || !out) return SPD_ERR_ARG;
+  std::unique_ptr<spd_ensemble> holder(new spd_ensemble());
+  spd_ensemble* E = holder.get();
+  E->steps_per_launch = steps_per_launch;
+  for (int i = 0; i < n; ++i) {
+    spd_ctx* C = ctxs[i];
+    if (!C) return efail(E, SPD_ERR_ARG, "null context");
+    if (C->recording || C->tape_mode != 0)
+      return efail(E, SPD_ERR_ARG, "packed ensembles do not record adjoint intermediates or decision tapes");
+    if (C->D != ctxs[0]->D || C->P != ctxs[0]->P || C->T != ctxs[0]->T)
+      return efail(E, SPD_ERR_ARG, "packed ensembles need one dimension, degree and time order");
+    E->ctx.push_back(C);
+    if (!C->t_dev) {
+      void* p = nullptr;
+      ECK(cudaMalloc(&p, sizeof(double)));
+      C->allocs.push_back(p);
+      C->t_dev = static_cast<double*>(p);
+    }
+    ECK(cudaStreamSynchronize(C->stream));
+    ECK(cudaMemset(C->t_dev, 0, sizeof(double)));
+  }
+  // record each instance's launch sequence (nothing is issued) and merge the
+  // i-th launch of every instance into one batched launch
+  E->packed.reset(new spd_batch::BatchRec());
+  spd_batch::BatchRec* R = E->packed.get();
+  for (int i = 0; i < n && R->err.empty(); ++i) {
+    spd_ctx* C = E->ctx[i];
+    const bool prof = C->prof;
+    C->prof = false;
+    C->brec = R;
+    R->begin_instance(i == 0);
+    int rc = 0;
+    for (int step = 0; step < steps_per_launch && !rc && R->err.empty(); ++step) {
+      rc = C->stepper->cmax(C);
+      if (!rc) rc = C->stepper->update(C);
+      if (!rc) launch<TimeAdd>(C, "k_time_add", k_time_add, 1, 1, 0, C->t_dev, C->dt);
+    }
+    C->brec = nullptr;
+    C->prof = prof;
+    if (rc) return efail(E, rc, std::string("recording instance ") + std::to_string(i) + ": " + C->err);
+    R->end_instance();
+  }
+  if (!R->err.empty()) return efail(E, SPD_ERR_ARG, R->err);
+  ECK(R->upload());
+  ECK(cudaStreamCreateWithFlags(&E->main, cudaStreamNonBlocking));
+  ECK(cudaStreamBeginCapture(E->main, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t el = R->launch(E->main);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(E->main, &g);
+  if (el != cudaSuccess || ec != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return efail(E, SPD_ERR_CUDA,
+                 std::string("capture: ") + cudaGetErrorString(el != cudaSuccess ? el : ec));
+  }
+  E->graph = g;
+  ECK(cudaGraphInstantiate(&E->exec, E->graph, 0));
+  for (spd_ctx* C : E->ctx) {
+    E->roles.push_back(C->U_cv);
+    E->roles.push_back(C->U_new);
+    E->roles.push_back(C->theta_final);
+  }
+  *out = holder.release();
+  return SPD_OK;
+}
+
+int spd_ensemble_graph_nodes(const spd_ensemble* E, long long* nodes) {
+  if (!E || !nodes) return SPD_ERR_ARG;
+  size_t n = 0;
+  if (E->graph && cudaGraphGetNodes(E->graph, nullptr, &n) != cudaSuccess) return SPD_ERR_CUDA;
+  *nodes = (long long)n;
+  return SPD_OK;
+}
+
 int spd_ensemble_step(spd_ensemble* E, int nlaunch) {
   if (!E || nlaunch < 0) return SPD_ERR_ARG;
   for (int i = 0; i < nlaunch; ++i) ECK(cudaGraphLaunch(E->exec, E->main));
@@ -173,7 +265,7 @@ int spd_ensemble_destroy(spd_ensemble* E) {
   return SPD_OK;
 }
 
-const char* spd_ensemble_last_error(const spd_ensemble* E) { return E ? E->err.c_str() : "null ensemble"; }
+const char* spd_ensemble_last_error(const spd_ensemble* E) { return E ? E->err.c_str() : t_last_err.c_str(); }
 
 int spd_set_cells_per_block(spd_ctx* C, int cpb) {
   if (!C || cpb < 1 || cpb > C->stepper->max_cpb || (cpb & (cpb - 1))) return SPD_ERR_ARG;

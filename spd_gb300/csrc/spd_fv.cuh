@@ -82,12 +82,13 @@ __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, i
 // W_new into the extended arrays (src/sdader_simulator.py:336-340,
 // src/trouble_detection.py:10-13)
 template <int D>
-__global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i,
-                               const double* F0, const double* F1, const double* F2,
-                               const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
-                               double* ext_new, int write_ext) {
+struct FvCandidate {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, const double* __restrict__ dt_ptr,
+                                           double w_i, const double* F0, const double* F1, const double* F2,
+                                           const double* __restrict__ U_cv, double* __restrict__ U_new,
+                                           double* ext_old, double* ext_new, int write_ext) {
   constexpr int V = D + 2;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nq) return;
   int ix, iy, iz;
   q_coords(g, q, ix, iy, iz);
@@ -114,6 +115,14 @@ __global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_pt
     for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
   }
 }
+};
+template <int D>
+__global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i,
+                               const double* F0, const double* F1, const double* F2,
+                               const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
+                               double* ext_new, int write_ext) {
+  FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext);
+}
 
 // ghost fill of one direction (src/fv_simulator.py:224-273): store the
 // boundary buffer when the reference does, then copy it into the ghost
@@ -121,13 +130,15 @@ __global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_pt
 // the remaining directions (lower direction fastest).  When ``gate`` is
 // non-null the fill runs only if *gate != 0.
 template <int D>
-__global__ void k_ghost(Geo g, int d, int all, int nv, int nv_buf, double* ext, double* bcbuf, const int* gate) {
+struct Ghost {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int all, int nv, int nv_buf, double* ext,
+                                           double* bcbuf, const int* gate) {
   if (gate != nullptr && *gate == 0) return;
   const int o0 = (d == 0) ? 1 : 0;
   const int o1 = (d == 2) ? 1 : 2;
   const long long nother = (long long)g.Xe[o0] * g.Xe[o1];
   const long long total = 2LL * nv * NGH * nother;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
   if (tid >= total) return;
   const long long other = tid % nother;
   long long r = tid / nother;
@@ -165,14 +176,24 @@ __global__ void k_ghost(Geo g, int d, int all, int nv, int nv_buf, double* ext, 
   const int dst = (side == 0) ? gi : Xd + NGH + gi;
   ext[(long long)v * g.Nqe + ext_index(dst)] = val;
 }
+};
+template <int D>
+__global__ void k_ghost(Geo g, int d, int all, int nv, int nv_buf, double* ext, double* bcbuf, const int* gate) {
+  Ghost<D>::run(hw_blk(), g, d, all, nv, nv_buf, ext, bcbuf, gate);
+}
 
 // NAD: relaxed discrete maximum principle over the cross stencil
 // (src/trouble_detection.py:14-38).  mask bit v = possible trouble of var v.
 template <int D>
-__global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __restrict__ ext_old,
-                      const double* __restrict__ ext_new, unsigned char* __restrict__ mask, int* any_flag) {
+struct Nad {
+// With sed_list non-null, the flagged (subcell, density / pressure) pairs
+// are also appended to sed_list (item 2*q + is_pressure) for k_sed.
+static __device__ __forceinline__ void run(Blk B, const Geo& g, double tol, int delta, int relax,
+                                           const double* __restrict__ ext_old, const double* __restrict__ ext_new,
+                                           unsigned char* __restrict__ mask, int* any_flag,
+                                           long long* __restrict__ sed_list, unsigned long long* __restrict__ sed_count) {
   constexpr int V = D + 2;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   unsigned int m = 0;
   if (q < g.Nq) {
     int ix, iy, iz;
@@ -215,6 +236,27 @@ __global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __r
   }
   const unsigned ballot = __ballot_sync(0xffffffffu, m != 0);
   if (ballot != 0 && (threadIdx.x & 31) == 0) atomicOr(any_flag, 1);
+  if (sed_list != nullptr && ballot != 0) {
+    constexpr int P_ = D + 1;
+    const bool f0 = m & 1u, fP = (m >> P_) & 1u;
+    const unsigned b0 = __ballot_sync(0xffffffffu, f0), bP = __ballot_sync(0xffffffffu, fP);
+    if (b0 | bP) {
+      const int lane = threadIdx.x & 31;
+      const unsigned lt = (1u << lane) - 1u;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(sed_count, (unsigned long long)(__popc(b0) + __popc(bP)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (f0) sed_list[base + __popc(b0 & lt)] = 2 * q;
+      if (fP) sed_list[base + __popc(b0) + __popc(bP & lt)] = 2 * q + 1;
+    }
+  }
+}
+};
+template <int D>
+__global__ void k_nad(Geo g, double tol, int delta, int relax, const double* __restrict__ ext_old,
+                      const double* __restrict__ ext_new, unsigned char* __restrict__ mask, int* any_flag,
+                      long long* __restrict__ sed_list, unsigned long long* __restrict__ sed_count) {
+  Nad<D>::run(hw_blk(), g, tol, delta, relax, ext_old, ext_new, mask, any_flag, sed_list, sed_count);
 }
 
 // smooth-extrema relaxation factor of one variable along direction d at
@@ -266,39 +308,66 @@ __device__ __forceinline__ double sed_alpha_dir(const double* W, long long e0, l
   return np_min(A(k - 1), np_min(A(k), A(k + 1)));
 }
 
-// SED + trouble flags + PAD (src/trouble_detection.py:40-70); writes the
-// troubles into var 0 of the theta-source extended array and the troubles
-// array.
+// SED (k_sed) and the trouble flags with PAD (k_troubles),
+// src/trouble_detection.py:40-70.
 template <int D>
-__global__ void k_troubles(Geo g, FvGeo fg, int sed_enabled, int pad, double min_rho, double max_rho, double min_P,
-                           const unsigned char* __restrict__ mask, const int* __restrict__ any_flag,
-                           const double* __restrict__ ext_new, double* __restrict__ theta_src,
-                           double* __restrict__ troubles) {
+struct Sed {
+// smooth-extrema relaxation of the NAD flags of density and pressure: one
+// list item per flagged (subcell, variable) pair, item = 2*q + (variable is
+// pressure), compacted by k_nad so that this FP64 work runs on full warps.
+// A pair whose smoothness indicator alpha is not < 1 clears its bit of the
+// NAD mask (bytes of one 32-bit word may belong to other items, hence the
+// atomic AND).
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, const long long* __restrict__ list,
+                                           const unsigned long long* __restrict__ count,
+                                           const double* __restrict__ ext_new, unsigned char* mask) {
   constexpr int P_ = D + 1;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const unsigned long long cnt = *count;
+  for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)B.n * blockDim.x) {
+    const long long item = list[idx];
+    const long long q = item >> 1;
+    const int var = (item & 1) ? P_ : 0;
+    int ix, iy, iz;
+    q_coords(g, q, ix, iy, iz);
+    const long long e = ext_of<D>(g, ix, iy, iz);
+    const int ii[3] = {ix, iy, iz};
+    const double* W = ext_new + (long long)var * g.Nqe;
+    double alpha = W[e] * 0.0 + 1.0;
+    for (int d = 0; d < D; ++d) {
+      const long long st = ext_stride(g, d);
+      const long long e0 = e - (long long)(ii[d] + NGH) * st;
+      const double an = sed_alpha_dir(W, e0, st, ii[d], g.X[d], fg.c2[d], fg.rc2[d], fg.hfp[d]);
+      alpha = (an < alpha) ? an : alpha;
+    }
+    if (!(alpha < 1.0))
+      atomicAnd(reinterpret_cast<unsigned*>(mask) + (q >> 2), ~(1u << (8 * (unsigned)(q & 3) + var)));
+  }
+}
+};
+template <int D>
+__global__ void k_sed(Geo g, FvGeo fg, const long long* __restrict__ list, const unsigned long long* __restrict__ count,
+                      const double* __restrict__ ext_new, unsigned char* mask) {
+  Sed<D>::run(hw_blk(), g, fg, list, count, ext_new, mask);
+}
+
+// trouble flags (NAD flags of density or pressure after the smooth-extrema
+// relaxation) and PAD; writes the troubles into var 0 of the theta-source
+// extended array and the troubles array.
+template <int D>
+struct Troubles {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double min_rho, double max_rho, double min_P,
+                                           const unsigned char* __restrict__ mask,
+                                           const double* __restrict__ ext_new, double* __restrict__ theta_src,
+                                           double* __restrict__ troubles) {
+  constexpr int P_ = D + 1;
+  const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nq) return;
   int ix, iy, iz;
   q_coords(g, q, ix, iy, iz);
   const long long e = ext_of<D>(g, ix, iy, iz);
   const unsigned m = mask[q];
-  int pt0 = m & 1u, ptP = (m >> P_) & 1u;
-  if (sed_enabled && *any_flag && (pt0 || ptP)) {
-    const int ii[3] = {ix, iy, iz};
-    const int vars[2] = {0, P_};
-    int* pts[2] = {&pt0, &ptP};
-    for (int w = 0; w < 2; ++w) {
-      if (!*pts[w]) continue;
-      const double* W = ext_new + (long long)vars[w] * g.Nqe;
-      double alpha = W[e] * 0.0 + 1.0;
-      for (int d = 0; d < D; ++d) {
-        const long long st = ext_stride(g, d);
-        const long long e0 = e - (long long)(ii[d] + NGH) * st;
-        const double an = sed_alpha_dir(W, e0, st, ii[d], g.X[d], fg.c2[d], fg.rc2[d], fg.hfp[d]);
-        alpha = (an < alpha) ? an : alpha;
-      }
-      *pts[w] = (alpha < 1.0) ? *pts[w] : 0;
-    }
-  }
+  const int pt0 = m & 1u, ptP = (m >> P_) & 1u;
   double t = (pt0 > ptP) ? (double)pt0 : (double)ptP;
   if (pad) {
     const double r = ext_new[e];
@@ -309,6 +378,13 @@ __global__ void k_troubles(Geo g, FvGeo fg, int sed_enabled, int pad, double min
   }
   theta_src[e] = t;
   troubles[q] = t;
+}
+};
+template <int D>
+__global__ void k_troubles(Geo g, int pad, double min_rho, double max_rho, double min_P,
+                           const unsigned char* __restrict__ mask, const double* __restrict__ ext_new,
+                           double* __restrict__ theta_src, double* __restrict__ troubles) {
+  Troubles<D>::run(hw_blk(), g, pad, min_rho, max_rho, min_P, mask, ext_new, theta_src, troubles);
 }
 
 // extended-grid coordinates
@@ -323,8 +399,10 @@ __device__ __forceinline__ void e_coords(const Geo& g, long long e, int& xe, int
 // 139-164); the 3D neighbour pairs are those the reference's index tuples
 // select.
 template <int D>
-__global__ void k_blend_neighbours(Geo g, const double* __restrict__ src, double* __restrict__ out) {
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+struct BlendNeighbours {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ src,
+                                           double* __restrict__ out) {
+  const long long e = B.id * (long long)blockDim.x + threadIdx.x;
   if (e >= g.Nqe) return;
   int c[3];
   e_coords(g, e, c[0], c[1], c[2]);
@@ -375,12 +453,19 @@ __global__ void k_blend_neighbours(Geo g, const double* __restrict__ src, double
   }
   out[e] = th;
 }
+};
+template <int D>
+__global__ void k_blend_neighbours(Geo g, const double* __restrict__ src, double* __restrict__ out) {
+  BlendNeighbours<D>::run(hw_blk(), g, src, out);
+}
 
 // last blending layer along direction d (src/trouble_detection.py:167-169):
 // two sequential in-place sweeps, fused with a one-cell halo.
 template <int D>
-__global__ void k_blend_last(Geo g, int d, const double* __restrict__ in, double* __restrict__ out) {
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+struct BlendLast {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, const double* __restrict__ in,
+                                           double* __restrict__ out) {
+  const long long e = B.id * (long long)blockDim.x + threadIdx.x;
   if (e >= g.Nqe) return;
   int c[3];
   e_coords(g, e, c[0], c[1], c[2]);
@@ -400,17 +485,24 @@ __global__ void k_blend_last(Geo g, int d, const double* __restrict__ in, double
     out[e] = a0;
   }
 }
+};
+template <int D>
+__global__ void k_blend_last(Geo g, int d, const double* __restrict__ in, double* __restrict__ out) {
+  BlendLast<D>::run(hw_blk(), g, d, in, out);
+}
 
 // affected faces of direction d (src/trouble_detection.py:81-87) and the
 // marks for the fallback fluxes and the corrected update.  With theta ==
 // nullptr the affected faces already in ``aff`` are used (replayed
 // decisions).
 template <int D>
-__global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__ theta, double* __restrict__ aff,
-                           unsigned char* __restrict__ mark_cell, unsigned char* __restrict__ mark_q,
-                           int* __restrict__ nmarked) {
+struct Affected {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int godunov, const double* __restrict__ theta,
+                                           double* __restrict__ aff, unsigned char* __restrict__ mark_cell,
+                                           unsigned char* __restrict__ mark_q, int* __restrict__ nmarked,
+                                           long long* __restrict__ flist, unsigned long long* __restrict__ fcount) {
   const long long nf = n_faces(g, d);
-  const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long fidx = B.id * (long long)blockDim.x + threadIdx.x;
   bool need = false;
   if (fidx < nf) {
     const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
@@ -452,36 +544,65 @@ __global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__
     }
   }
   const unsigned b = __ballot_sync(0xffffffffu, need);
-  if (b != 0 && (threadIdx.x & 31) == 0) atomicAdd(nmarked, __popc(b));
+  if (b != 0) {
+    // the faces that need a fallback flux, compacted by warp ballot: an FP64
+    // warp instruction costs the same with 1 or 32 active lanes, so the
+    // fallback Riemann problems run on full warps over this list
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) {
+      atomicAdd(nmarked, __popc(b));
+      base = atomicAdd(fcount, (unsigned long long)__popc(b));
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) flist[base + __popc(b & ((1u << lane) - 1u))] = fidx;
+  }
+}
+};
+template <int D>
+__global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__ theta, double* __restrict__ aff,
+                           unsigned char* __restrict__ mark_cell, unsigned char* __restrict__ mark_q,
+                           int* __restrict__ nmarked, long long* __restrict__ flist,
+                           unsigned long long* __restrict__ fcount) {
+  Affected<D>::run(hw_blk(), g, d, godunov, theta, aff, mark_cell, mark_q, nmarked, flist, fcount);
 }
 
 // compaction of marked indices by warp ballot: writes the marked indices
 // into list and their count into *count.
+struct Compact {
+  static __device__ __forceinline__ void run(Blk B, long long total, const unsigned char* __restrict__ mark,
+                                             long long* __restrict__ list, unsigned long long* __restrict__ count) {
+    const long long i = B.id * (long long)blockDim.x + threadIdx.x;
+    const bool m = (i < total) && mark[i];
+    const unsigned b = __ballot_sync(0xffffffffu, m);
+    if (b == 0) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (m) list[base + __popc(b & ((1u << lane) - 1u))] = i;
+  }
+};
 static __global__ void k_compact(long long total, const unsigned char* __restrict__ mark, long long* __restrict__ list,
                           unsigned long long* __restrict__ count) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const bool m = (i < total) && mark[i];
-  const unsigned b = __ballot_sync(0xffffffffu, m);
-  if (b == 0) return;
-  const int lane = threadIdx.x & 31;
-  unsigned long long base = 0;
-  if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(b));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (m) list[base + __popc(b & ((1u << lane) - 1u))] = i;
+  Compact::run(hw_blk(), total, mark, list, count);
 }
 
 // MUSCL-Hancock: limited gradients, slopes and the half-step primitive
 // predictor of one extended subcell (src/muscl.py:61-75,129-173,175-216).
 template <int D, int BM = 0>
-__global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __restrict__ dt_ptr, double w_i,
-                              const long long* __restrict__ list, const unsigned long long* __restrict__ count,
-                              const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S,
-                              unsigned char* ltape = nullptr) {
+struct MusclCells {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, int limiter,
+                                           const double* __restrict__ dt_ptr, double w_i,
+                                           const long long* __restrict__ list,
+                                           const unsigned long long* __restrict__ count,
+                                           const double* __restrict__ W_ext, double* __restrict__ Mpred,
+                                           double* __restrict__ S, unsigned char* ltape) {
   constexpr int V = D + 2, P_ = D + 1;
   const unsigned long long cnt = *count;
   const double dti = *dt_ptr * w_i;
-  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
-       idx += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)B.n * blockDim.x) {
   const long long e = list[idx];
   int c[3];
   e_coords(g, e, c[0], c[1], c[2]);
@@ -524,19 +645,36 @@ __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __rest
   for (int v = 0; v < V; ++v) Mpred[(long long)v * g.Nqe + e] = W[v] + 0.5 * dtW[v] * dti;
   }
 }
+};
+template <int D, int BM = 0>
+__global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __restrict__ dt_ptr, double w_i,
+                              const long long* __restrict__ list, const unsigned long long* __restrict__ count,
+                              const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S,
+                              unsigned char* ltape = nullptr) {
+  MusclCells<D, BM>::run(hw_blk(), g, fg, limiter, dt_ptr, w_i, list, count, W_ext, Mpred, S, ltape);
+}
 
 // fallback Riemann flux on the affected faces of direction d
 // (src/muscl.py:217-221, src/fv_simulator.py:88-165)
 template <int D, int BM = 0>
-__global__ void k_muscl_faces(Geo g, int d, int solver, int godunov, const double* __restrict__ aff,
-                              const double* __restrict__ Mpred, const double* __restrict__ S,
-                              double* __restrict__ F_FB, unsigned* ftape = nullptr) {
+struct MusclFaces {
+// the affected faces of direction d from their compacted list (k_affected),
+// a grid-stride loop over full warps
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int solver,
+                                           const long long* __restrict__ flist,
+                                           const unsigned long long* __restrict__ fcount,
+                                           const double* __restrict__ Mpred, const double* __restrict__ S,
+                                           double* __restrict__ F_FB, unsigned* ftape) {
+  const unsigned long long cnt = *fcount;
+  for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)B.n * blockDim.x)
+    face(g, d, solver, flist[idx], Mpred, S, F_FB, ftape);
+}
+static __device__ __forceinline__ void face(const Geo& g, int d, int solver, long long fidx,
+                                            const double* __restrict__ Mpred, const double* __restrict__ S,
+                                            double* __restrict__ F_FB, unsigned* ftape) {
   constexpr int V = D + 2;
   const long long nf = n_faces(g, d);
-  const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (fidx >= nf) return;
-  const double a = aff[fidx];
-  if (!(godunov || a != 0.0)) return;
   const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
   int f[3];
   f[0] = (int)(fidx % FX);
@@ -561,23 +699,32 @@ __global__ void k_muscl_faces(Geo g, int d, int solver, int godunov, const doubl
 #pragma unroll
   for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = F[v];
 }
+};
+template <int D, int BM = 0>
+__global__ void k_muscl_faces(Geo g, int d, int solver, const long long* __restrict__ flist,
+                              const unsigned long long* __restrict__ fcount, const double* __restrict__ Mpred,
+                              const double* __restrict__ S, double* __restrict__ F_FB, unsigned* ftape = nullptr) {
+  MusclFaces<D, BM>::run(hw_blk(), g, d, solver, flist, fcount, Mpred, S, F_FB, ftape);
+}
 
 // corrected update of the subcells next to an affected face
 // (src/sdader_simulator.py:325-331,346)
 template <int D>
-__global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i, int godunov,
-                             const long long* __restrict__ list, const unsigned long long* __restrict__ count,
-                             const double* F0, const double* F1, const double* F2, const double* B0,
-                             const double* B1, const double* B2, const double* A0, const double* A1,
-                             const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new) {
+struct FvCorrect {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, const double* __restrict__ dt_ptr,
+                                           double w_i, int godunov, const long long* __restrict__ list,
+                                           const unsigned long long* __restrict__ count, const double* F0,
+                                           const double* F1, const double* F2, const double* B0, const double* B1,
+                                           const double* B2, const double* A0, const double* A1, const double* A2,
+                                           const double* __restrict__ U_cv, double* __restrict__ U_new) {
   constexpr int V = D + 2;
   const unsigned long long cnt = *count;
   const double* FH[3] = {F0, F1, F2};
   const double* FB[3] = {B0, B1, B2};
   const double* AF[3] = {A0, A1, A2};
   const double dti = *dt_ptr * w_i;
-  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
-       idx += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)B.n * blockDim.x) {
   const long long q = list[idx];
   int ix, iy, iz;
   q_coords(g, q, ix, iy, iz);
@@ -606,15 +753,32 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
   }
   }
 }
+};
+template <int D>
+__global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i, int godunov,
+                             const long long* __restrict__ list, const unsigned long long* __restrict__ count,
+                             const double* F0, const double* F1, const double* F2, const double* B0,
+                             const double* B1, const double* B2, const double* A0, const double* A1,
+                             const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new) {
+  FvCorrect<D>::run(hw_blk(), g, fg, dt_ptr, w_i, godunov, list, count, F0, F1, F2, B0, B1, B2, A0, A1, A2, U_cv,
+                    U_new);
+}
 
 // dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when
 // a NaN entered the reduction) (src/sd_simulator.py:214-227)
+struct DtFinal {
+  static __device__ __forceinline__ void run(Blk, double h, double cfl, const unsigned long long* cmax_bits,
+                                             const int* nan_flag, double* dt) {
+    if (threadIdx.x != 0) return;
+    const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
+                                  : __longlong_as_double((long long)*cmax_bits);
+    const double dtt = h / cmax;
+    *dt = cfl * dtt;
+  }
+};
 static __global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
                            double* dt) {
-  const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
-                                : __longlong_as_double((long long)*cmax_bits);
-  const double dtt = h / cmax;
-  *dt = cfl * dtt;
+  DtFinal::run(hw_blk(), h, cfl, cmax_bits, nan_flag, dt);
 }
 
 }  // namespace spd

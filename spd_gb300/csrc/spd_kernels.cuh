@@ -104,12 +104,22 @@ __device__ __forceinline__ void write_traces(const Ops& op, const Geo& g, const 
   }
 }
 
+// Every kernel of the step is a body ``run(Blk, args...)`` plus a plain
+// ``__global__`` wrapper that passes the hardware block index; the batched
+// ensemble launches the same bodies over many instances at once.
+template <int D, int P>
+struct TracesSp {
+  static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, const double* __restrict__ U_sp,
+                                             double* t0, double* t1, double* t2) {
+    const long long c = B.id * (long long)blockDim.x + threadIdx.x;
+    if (c >= g.Nc) return;
+    double* tr[3] = {t0, t1, t2};
+    write_traces<D, P>(op, g, U_sp, 1, 0, c, tr, 0);
+  }
+};
 template <int D, int P>
 __global__ void k_traces_sp(Ops op, Geo g, const double* __restrict__ U_sp, double* t0, double* t1, double* t2) {
-  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (c >= g.Nc) return;
-  double* tr[3] = {t0, t1, t2};
-  write_traces<D, P>(op, g, U_sp, 1, 0, c, tr, 0);
+  TracesSp<D, P>::run(hw_blk(), op, g, U_sp, t0, t1, t2);
 }
 
 // traces of every (cell, time node) of an iterate U (Tu time nodes stored)
@@ -131,13 +141,15 @@ __global__ void k_traces_ader(Ops op, Geo g, const double* __restrict__ U, int T
 // DIR >= 0 fixes the direction at compile time (the rotated velocity
 // indices become constants); DIR = -1 takes it from d_rt.
 template <int D, int P, int BM = 0, int DIR = -1>
-__global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
-                             const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape = nullptr) {
+struct RiemannSd {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Teff, int solver,
+                                           const double* __restrict__ trace, const double* __restrict__ bcfix,
+                                           double* __restrict__ Fi, unsigned* tape) {
   using k = K<D, P>;
   const int d = (DIR >= 0) ? DIR : d_rt;
   const long long nI = n_iface(g, d);
   const long long total = (long long)Teff * k::NJ * nI;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
   if (tid >= total) return;
   const long long iface = tid % nI;
   const long long r = tid / nI;
@@ -220,6 +232,12 @@ __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double
 #pragma unroll
   for (int v = 0; v < k::V; ++v) Fi[(((long long)v * g.T + t) * k::NJ + j) * nI + iface] = F[v];
 }
+};
+template <int D, int P, int BM = 0, int DIR = -1>
+__global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
+                             const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape = nullptr) {
+  RiemannSd<D, P, BM, DIR>::run(hw_blk(), g, d_rt, Teff, solver, trace, bcfix, Fi, tape);
+}
 
 // ---------------------------------------------------------------------------
 // interior flux points, derivative, Picard update (src/sdader_simulator.py:
@@ -229,15 +247,17 @@ __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double
 //       2 = write Ffp.
 // ---------------------------------------------------------------------------
 template <int D, int P>
-__global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
-                           const double* __restrict__ dt_ptr, double* __restrict__ U_sp, double* __restrict__ U_ader,
-                           const double* Fi0, const double* Fi1, const double* Fi2, double* tr0, double* tr1,
-                           double* tr2, double* Ffp0, double* Ffp1, double* Ffp2) {
+struct Interior {
+static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int mode, int Teff,
+                                           const double* __restrict__ Uin, int Tu, const double* __restrict__ dt_ptr,
+                                           double* __restrict__ U_sp, double* __restrict__ U_ader, const double* Fi0,
+                                           const double* Fi1, const double* Fi2, double* tr0, double* tr1,
+                                           double* tr2, double* Ffp0, double* Ffp1, double* Ffp2) {
   using k = K<D, P>;
   extern __shared__ double dudt_s[];  // [(v*NS + s)*Teff + tl][CPB]
   const int CPB = blockDim.x;
   const int cl = threadIdx.x, tl = threadIdx.y;
-  const long long c = blockIdx.x * (long long)CPB + cl;
+  const long long c = B.id * (long long)CPB + cl;
   const bool active = c < g.Nc;
   const double* Fi[3] = {Fi0, Fi1, Fi2};
   double* Ffp[3] = {Ffp0, Ffp1, Ffp2};
@@ -328,6 +348,15 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
     }
   }
 }
+};
+template <int D, int P>
+__global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
+                           const double* __restrict__ dt_ptr, double* __restrict__ U_sp, double* __restrict__ U_ader,
+                           const double* Fi0, const double* Fi1, const double* Fi2, double* tr0, double* tr1,
+                           double* tr2, double* Ffp0, double* Ffp1, double* Ffp2) {
+  Interior<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2, Ffp0,
+                      Ffp1, Ffp2);
+}
 
 // ---------------------------------------------------------------------------
 // transverse subcell averaging of the flux points and scatter to the FV face
@@ -336,10 +365,12 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
 // F_HO layout [t][v][face], faces x-fastest with X_d + 1 along d.
 // ---------------------------------------------------------------------------
 template <int D, int P>
-__global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict__ Ffp, double* __restrict__ F_HO) {
+struct IntegrateFaces {
+static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int d, const double* __restrict__ Ffp,
+                                           double* __restrict__ F_HO) {
   using k = K<D, P>;
   const long long total = g.Nc * g.T * k::nf;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
   if (tid >= total) return;
   const long long c = tid % g.Nc;
   const long long r = tid / g.Nc;
@@ -401,6 +432,11 @@ __global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict
     }
   }
 }
+};
+template <int D, int P>
+__global__ void k_integrate_faces(Ops op, Geo g, int d, const double* __restrict__ Ffp, double* __restrict__ F_HO) {
+  IntegrateFaces<D, P>::run(hw_blk(), op, g, d, Ffp, F_HO);
+}
 
 // ---------------------------------------------------------------------------
 // whole-cell transforms sp <-> subcell averages (src/transforms.py:27-45)
@@ -431,10 +467,11 @@ __device__ __forceinline__ double full_dot(const double* __restrict__ Krow, cons
 
 // U_cv (FV layout) = sp_to_cv(U_sp) for every cell and variable
 template <int D, int P>
-__global__ void k_sp_to_cv(Geo g, const double* __restrict__ Kfull, const double* __restrict__ U_sp,
-                           double* __restrict__ U_cv) {
+struct SpToCv {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ Kfull,
+                                           const double* __restrict__ U_sp, double* __restrict__ U_cv) {
   using k = K<D, P>;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
   if (tid >= g.Nc * k::V) return;
   const long long c = tid % g.Nc;
   const int v = (int)(tid / g.Nc);
@@ -450,13 +487,20 @@ __global__ void k_sp_to_cv(Geo g, const double* __restrict__ Kfull, const double
     U_cv[(long long)v * g.Nq + q] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, false);
   }
 }
+};
+template <int D, int P>
+__global__ void k_sp_to_cv(Geo g, const double* __restrict__ Kfull, const double* __restrict__ U_sp,
+                           double* __restrict__ U_cv) {
+  SpToCv<D, P>::run(hw_blk(), g, Kfull, U_sp, U_cv);
+}
 
 // U_sp = cv_to_sp(U_cv) (strided view order)
 template <int D, int P>
-__global__ void k_cv_to_sp(Geo g, const double* __restrict__ Kfull, const double* __restrict__ U_cv,
-                           double* __restrict__ U_sp) {
+struct CvToSp {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ Kfull,
+                                           const double* __restrict__ U_cv, double* __restrict__ U_sp) {
   using k = K<D, P>;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
   if (tid >= g.Nc * k::V) return;
   const long long c = tid % g.Nc;
   const int v = (int)(tid / g.Nc);
@@ -471,6 +515,12 @@ __global__ void k_cv_to_sp(Geo g, const double* __restrict__ Kfull, const double
     x[s] = U_cv[(long long)v * g.Nq + q];
   }
   for (int o = 0; o < k::NS; ++o) U_sp[((long long)v * k::NS + o) * g.Nc + c] = full_dot<D, P>(Kfull + (long long)o * k::NS, x, true);
+}
+};
+template <int D, int P>
+__global__ void k_cv_to_sp(Geo g, const double* __restrict__ Kfull, const double* __restrict__ U_cv,
+                           double* __restrict__ U_sp) {
+  CvToSp<D, P>::run(hw_blk(), g, Kfull, U_cv, U_sp);
 }
 
 }  // namespace spd

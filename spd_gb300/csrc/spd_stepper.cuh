@@ -10,10 +10,11 @@ template <int D, int P>
 int adjoint_vjp(spd_ctx* C);
 
 template <int D, int P>
-__global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned long long* __restrict__ cmax_bits,
-                            int* __restrict__ nan_flag) {
+struct CmaxOnly {
+static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ W_cv,
+                                           unsigned long long* __restrict__ cmax_bits, int* __restrict__ nan_flag) {
   constexpr int P_ = D + 1;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   double cval = 0.0;
   bool isnan_c = false;
   if (q < g.Nq) {
@@ -33,18 +34,31 @@ __global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned lon
     if (nb) atomicOr(nan_flag, 1);
   }
 }
+};
+template <int D, int P>
+__global__ void k_cmax_only(Geo g, const double* __restrict__ W_cv, unsigned long long* __restrict__ cmax_bits,
+                            int* __restrict__ nan_flag) {
+  CmaxOnly<D, P>::run(hw_blk(), g, W_cv, cmax_bits, nan_flag);
+}
 
 template <int D>
+struct PrimOnly {
+  static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ U_cv,
+                                             double* __restrict__ W_cv) {
+    constexpr int V = D + 2;
+    const long long q = B.id * (long long)blockDim.x + threadIdx.x;
+    if (q >= g.Nq) return;
+    double u[V], W[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
+    prim<D>(u, W, g.gamma, 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
+  }
+};
+template <int D>
 __global__ void k_prim_only(Geo g, const double* __restrict__ U_cv, double* __restrict__ W_cv) {
-  constexpr int V = D + 2;
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= g.Nq) return;
-  double u[V], W[V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
-  prim<D>(u, W, g.gamma, 0);
-#pragma unroll
-  for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
+  PrimOnly<D>::run(hw_blk(), g, U_cv, W_cv);
 }
 
 
@@ -71,8 +85,8 @@ struct Stepper : StepperBase {
                          C->stream));
     {
       ProfScope ps_(C, "k_traces_sp");
-      k_traces_sp<D, P><<<blocks_for(g.Nc, 128), 128, 0, C->stream>>>(C->ops, g, C->U_sp, C->trace[0], C->trace[1],
-                                                                     C->trace[2]);
+      launch<TracesSp<D, P>>(C, "k_traces_sp", k_traces_sp<D, P>, blocks_for(g.Nc, 128), 128, 0, C->ops, g, C->U_sp,
+                             C->trace[0], C->trace[1], C->trace[2]);
     }
     CKL();
     const int m = C->T - 1;
@@ -85,15 +99,17 @@ struct Stepper : StepperBase {
           ProfScope ps_(C, "k_riemann_sd");
           if (C->tape_mode == 0) {
             const unsigned nb = blocks_for(tot, 128);
+            constexpr int D1 = (D > 1 ? 1 : 0), D2 = (D > 2 ? 2 : 0);
+            unsigned* no_tape = nullptr;
             if (d == 0)
-              k_riemann_sd<D, P, 0, 0><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d], C->bcfix[d],
-                                                                  C->Fi[d]);
+              launch<RiemannSd<D, P, 0, 0>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, 0>, nb, 128, 0, g, d, Teff,
+                                            solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
             else if (d == 1)
-              k_riemann_sd<D, P, 0, (D > 1 ? 1 : 0)><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                C->bcfix[d], C->Fi[d]);
+              launch<RiemannSd<D, P, 0, D1>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D1>, nb, 128, 0, g, d, Teff,
+                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
             else
-              k_riemann_sd<D, P, 0, (D > 2 ? 2 : 0)><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                C->bcfix[d], C->Fi[d]);
+              launch<RiemannSd<D, P, 0, D2>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D2>, nb, 128, 0, g, d, Teff,
+                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
           } else {
             unsigned* tp = C->tape_rs[d] + ((size_t)C->tape_step * C->T + it) * C->T * k::NJ * n_iface(g, d);
             if (C->tape_mode == 1)
@@ -113,9 +129,9 @@ struct Stepper : StepperBase {
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
       {
         ProfScope ps_(C, "k_interior");
-        k_interior<D, P><<<blocks_for(g.Nc, cpb), block, sm, C->stream>>>(
-            C->ops, g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
-            C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2]);
+        launch<Interior<D, P>>(C, "k_interior", k_interior<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops, g, mode,
+                               Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
+                               C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2]);
       }
       CKL();
       if (C->recording && mode == 0) {
@@ -131,7 +147,8 @@ struct Stepper : StepperBase {
     const Geo& g = C->geo;
     {
       ProfScope ps_(C, "k_sp_to_cv");
-      k_sp_to_cv<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_sp_to_cv, C->U_sp, C->U_cv);
+      launch<SpToCv<D, P>>(C, "k_sp_to_cv", k_sp_to_cv<D, P>, blocks_for(g.Nc * k::V, 128), 128, 0, g, C->K_sp_to_cv,
+                           C->U_sp, C->U_cv);
     }
     CKL();
     return 0;
@@ -141,7 +158,7 @@ struct Stepper : StepperBase {
     const Geo& g = C->geo;
     {
       ProfScope ps_(C, "k_prim_only");
-      k_prim_only<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->U_cv, C->W_cv);
+      launch<PrimOnly<D>>(C, "k_prim_only", k_prim_only<D>, blocks_for(g.Nq, BS), BS, 0, g, C->U_cv, C->W_cv);
     }
     CKL();
     return 0;
@@ -149,16 +166,18 @@ struct Stepper : StepperBase {
 
   int cmax(spd_ctx* C) override {
     const Geo& g = C->geo;
-    CK(cudaMemsetAsync(C->flags + 1, 0, sizeof(int), C->stream));
-    CK(cudaMemsetAsync(C->counts + 2, 0, sizeof(unsigned long long), C->stream));
+    CK(zero_fill(C, C->flags + 1, sizeof(int)));
+    CK(zero_fill(C, C->counts + 2, sizeof(unsigned long long)));
     {
       ProfScope ps_(C, "k_cmax_only");
-      k_cmax_only<D, P><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->W_cv, C->counts + 2, C->flags + 1);
+      launch<CmaxOnly<D, P>>(C, "k_cmax_only", k_cmax_only<D, P>, blocks_for(g.Nq, BS), BS, 0, g, C->W_cv,
+                             C->counts + 2, C->flags + 1);
     }
     CKL();
     {
       ProfScope ps_(C, "k_dt_final");
-      k_dt_final<<<1, 1, 0, C->stream>>>(C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1, C->dt);
+      launch<DtFinal>(C, "k_dt_final", k_dt_final, 1, 1, 0, C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1,
+                      C->dt);
     }
     CKL();
     return 0;
@@ -182,8 +201,8 @@ struct Stepper : StepperBase {
     for (int d = 0; d < D; ++d) {
       {
         ProfScope ps_(C, "k_integrate_faces");
-        k_integrate_faces<D, P><<<blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->stream>>>(C->ops, g, d, C->Ffp[d],
-                                                                                            C->F_HO[d]);
+        launch<IntegrateFaces<D, P>>(C, "k_integrate_faces", k_integrate_faces<D, P>,
+                                     blocks_for(g.Nc * g.T * k::nf, 128), 128, 0, C->ops, g, d, C->Ffp[d], C->F_HO[d]);
       }
       CKL();
     }
@@ -198,9 +217,8 @@ struct Stepper : StepperBase {
       for (int d = 0; d < D; ++d) FH[d] = C->F_HO[d] + (long long)i * k::V * nface[d];
       {
         ProfScope ps_(C, "k_fv_candidate");
-        k_fv_candidate<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, C->dt, w_i, FH[0], FH[1], FH[2],
-                                                                       C->U_cv, C->U_new, C->ext_old, C->ext_new,
-                                                                       cf.FB ? 1 : 0);
+        launch<FvCandidate<D>>(C, "k_fv_candidate", k_fv_candidate<D>, blocks_for(g.Nq, BS), BS, 0, g, C->fvg, C->dt,
+                               w_i, FH[0], FH[1], FH[2], C->U_cv, C->U_new, C->ext_old, C->ext_new, cf.FB ? 1 : 0);
       }
       CKL();
       if (cf.FB && C->tape_mode == 2) {
@@ -219,24 +237,30 @@ struct Stepper : StepperBase {
         for (int d = 0; d < D; ++d) {
           if (int r = ghost(C, d, 1, k::V, C->ext_old, nullptr)) return r;
         }
-        CK(cudaMemsetAsync(C->flags, 0, sizeof(int), C->stream));
+        const int sed = (P > 1 && cf.SED) ? 1 : 0;
+        CK(zero_fill(C, C->flags, sizeof(int)));
+        if (sed) CK(zero_fill(C, C->counts + 3, sizeof(unsigned long long)));
         {
           ProfScope ps_(C, "k_nad");
-          k_nad<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, cf.tolerance, cf.NAD_delta, P > 0 ? 1 : 0, C->ext_old,
-                                                               C->ext_new, C->mask, C->flags);
+          long long* sed_list = sed ? C->list_sed : nullptr;
+          launch<Nad<D>>(C, "k_nad", k_nad<D>, blocks_for(g.Nq, BS), BS, 0, g, cf.tolerance, cf.NAD_delta,
+                         P > 0 ? 1 : 0, C->ext_old, C->ext_new, C->mask, C->flags, sed_list, C->counts + 3);
         }
         CKL();
-        const int sed = (P > 1 && cf.SED) ? 1 : 0;
         if (sed) {
           for (int d = 0; d < D; ++d) {
             if (int r = ghost(C, d, 1, k::V, C->ext_new, C->flags)) return r;
           }
+          ProfScope ps_(C, "k_sed");
+          const unsigned nb = (unsigned)std::min<long long>(PERSIST_BLOCKS, blocks_for(2 * g.Nq, BS));
+          launch<Sed<D>>(C, "k_sed", k_sed<D>, nb, BS, 0, g, C->fvg, C->list_sed, C->counts + 3, C->ext_new,
+                         C->mask);
+          CKL();
         }
         {
           ProfScope ps_(C, "k_troubles");
-          k_troubles<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, C->fvg, sed, cf.PAD, cf.min_rho, cf.max_rho,
-                                                                    cf.min_P, C->mask, C->flags, C->ext_new,
-                                                                    C->theta_src, C->troubles);
+          launch<Troubles<D>>(C, "k_troubles", k_troubles<D>, blocks_for(g.Nq, BS), BS, 0, g, cf.PAD, cf.min_rho,
+                              cf.max_rho, cf.min_P, C->mask, C->ext_new, C->theta_src, C->troubles);
         }
         CKL();
         for (int d = 0; d < D; ++d) {
@@ -246,7 +270,8 @@ struct Stepper : StepperBase {
         if (cf.blending) {
           {
             ProfScope ps_(C, "k_blend_neighbours");
-            k_blend_neighbours<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, C->theta_src, C->theta_a);
+            launch<BlendNeighbours<D>>(C, "k_blend_neighbours", k_blend_neighbours<D>, blocks_for(g.Nqe, BS), BS, 0, g,
+                                       C->theta_src, C->theta_a);
           }
           CKL();
           double* in = C->theta_a;
@@ -254,7 +279,7 @@ struct Stepper : StepperBase {
           for (int d = 0; d < D; ++d) {
             {
               ProfScope ps_(C, "k_blend_last");
-              k_blend_last<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, d, in, out);
+              launch<BlendLast<D>>(C, "k_blend_last", k_blend_last<D>, blocks_for(g.Nqe, BS), BS, 0, g, d, in, out);
             }
             CKL();
             std::swap(in, out);
@@ -265,27 +290,30 @@ struct Stepper : StepperBase {
       }
       if (cf.FB) {
         // affected faces, marks and the fallback fluxes (src/sdader_simulator.py:343-346)
-        CK(cudaMemsetAsync(C->mark_cell, 0, (size_t)g.Nqe, C->stream));
-        CK(cudaMemsetAsync(C->mark_q, 0, (size_t)g.Nq, C->stream));
-        CK(cudaMemsetAsync(C->counts, 0, 2 * sizeof(unsigned long long), C->stream));
+        CK(zero_fill(C, C->mark_cell, (size_t)g.Nqe));
+        CK(zero_fill(C, C->mark_q, (size_t)g.Nq));
+        CK(zero_fill(C, C->counts, 2 * sizeof(unsigned long long)));
+        CK(zero_fill(C, C->counts + 4, D * sizeof(unsigned long long)));
         for (int d = 0; d < D; ++d) {
           {
             ProfScope ps_(C, "k_affected");
-            k_affected<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.godunov,
-                                                                          C->tape_mode == 2 ? nullptr : C->theta_final,
-                                                                          C->aff[d],
-                                                                          C->mark_cell, C->mark_q, C->flags + 2);
+            const double* th = C->tape_mode == 2 ? nullptr : C->theta_final;
+            launch<Affected<D>>(C, "k_affected", k_affected<D>, blocks_for(nface[d], BS), BS, 0, g, d, cf.godunov, th,
+                                C->aff[d], C->mark_cell, C->mark_q, C->flags + 2, C->list_face[d],
+                                C->counts + 4 + d);
           }
           CKL();
         }
         {
           ProfScope ps_(C, "k_compact");
-          k_compact<<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g.Nqe, C->mark_cell, C->list_cell, C->counts);
+          launch<Compact>(C, "k_compact", k_compact, blocks_for(g.Nqe, BS), BS, 0, g.Nqe, C->mark_cell, C->list_cell,
+                          C->counts);
         }
         CKL();
         {
           ProfScope ps_(C, "k_compact");
-          k_compact<<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g.Nq, C->mark_q, C->list_q, C->counts + 1);
+          launch<Compact>(C, "k_compact", k_compact, blocks_for(g.Nq, BS), BS, 0, g.Nq, C->mark_q, C->list_q,
+                          C->counts + 1);
         }
         CKL();
         if (C->tape_mode == 1) {
@@ -307,17 +335,21 @@ struct Stepper : StepperBase {
         for (int d = 0; d < D; ++d) {
           {
             ProfScope ps_(C, "k_muscl_faces");
+            // grid-stride over the compacted list of affected faces
+            const unsigned nb = (unsigned)std::min<long long>(PERSIST_BLOCKS, blocks_for(nface[d], BS));
+            const unsigned long long* fcount = C->counts + 4 + d;
             if (C->tape_mode == 0) {
-              k_muscl_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, cf.godunov,
-                                                                               C->aff[d], C->Mpred, C->S, C->F_FB[d]);
+              unsigned* no_tape = nullptr;
+              launch<MusclFaces<D>>(C, "k_muscl_faces", k_muscl_faces<D>, nb, BS, 0, g, d, cf.riemann_solver_fv,
+                                    C->list_face[d], fcount, C->Mpred, C->S, C->F_FB[d], no_tape);
             } else {
               unsigned* tp = C->tape_fb[d] + ((size_t)C->tape_step * C->T + i) * nface[d];
               if (C->tape_mode == 1)
-                k_muscl_faces<D, 1><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(
-                    g, d, cf.riemann_solver_fv, cf.godunov, C->aff[d], C->Mpred, C->S, C->F_FB[d], tp);
+                k_muscl_faces<D, 1><<<nb, BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, C->list_face[d], fcount,
+                                                             C->Mpred, C->S, C->F_FB[d], tp);
               else
-                k_muscl_faces<D, 2><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(
-                    g, d, cf.riemann_solver_fv, cf.godunov, C->aff[d], C->Mpred, C->S, C->F_FB[d], tp);
+                k_muscl_faces<D, 2><<<nb, BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, C->list_face[d], fcount,
+                                                             C->Mpred, C->S, C->F_FB[d], tp);
             }
           }
           CKL();
@@ -340,7 +372,8 @@ struct Stepper : StepperBase {
     // switch_to_high_order (src/sdader_simulator.py:300-307)
     {
       ProfScope ps_(C, "k_cv_to_sp");
-      k_cv_to_sp<D, P><<<blocks_for(g.Nc * k::V, 128), 128, 0, C->stream>>>(g, C->K_cv_to_sp, C->U_cv, C->U_sp);
+      launch<CvToSp<D, P>>(C, "k_cv_to_sp", k_cv_to_sp<D, P>, blocks_for(g.Nc * k::V, 128), 128, 0, g, C->K_cv_to_sp,
+                           C->U_cv, C->U_sp);
     }
     CKL();
     return 0;
@@ -351,8 +384,10 @@ struct Stepper : StepperBase {
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nqe, 128));
     ProfScope ps_(C, "k_muscl_cells");
     if (C->tape_mode == 0) {
-      k_muscl_cells<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i, C->list_cell,
-                                                            C->counts, C->ext_old, C->Mpred, C->S);
+      unsigned char* no_tape = nullptr;
+      launch<MusclCells<D>>(C, "k_muscl_cells", k_muscl_cells<D>, (unsigned)nb, 128, 0, g, C->fvg,
+                            C->cfg.slope_limiter, C->dt, w_i, C->list_cell, C->counts, C->ext_old, C->Mpred, C->S,
+                            no_tape);
       return;
     }
     unsigned char* lt = C->tape_lim + ((size_t)C->tape_step * C->T + i) * D * k::V * g.Nqe;
@@ -369,10 +404,9 @@ struct Stepper : StepperBase {
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nq, 128));
     {
       ProfScope ps_(C, "k_fv_correct");
-      k_fv_correct<D><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->dt, w_i, C->cfg.godunov, C->list_q,
-                                                           C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
-                                                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv,
-                                                           C->U_new);
+      launch<FvCorrect<D>>(C, "k_fv_correct", k_fv_correct<D>, (unsigned)nb, 128, 0, g, C->fvg, C->dt, w_i,
+                           C->cfg.godunov, C->list_q, C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
+                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new);
     }
   }
 
@@ -383,7 +417,8 @@ struct Stepper : StepperBase {
     const long long tot = 2LL * nv * NGH * g.Xe[o0] * g.Xe[o1];
     {
       ProfScope ps_(C, "k_ghost");
-      k_ghost<D><<<blocks_for(tot, BS), BS, 0, C->stream>>>(g, d, all, nv, k::V, ext, C->bcbuf[d], gate);
+      launch<Ghost<D>>(C, "k_ghost", k_ghost<D>, blocks_for(tot, BS), BS, 0, g, d, all, nv, k::V, ext, C->bcbuf[d],
+                       gate);
     }
     CKL();
     return 0;

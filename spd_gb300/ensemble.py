@@ -2,13 +2,20 @@
 counterpart).
 
 ``SDADER_Ensemble`` advances many ``SDADER_Simulator`` instances of
-different grid sizes together: the step of every instance -- its own CFL
-reduction, predictor, FV update -- is recorded once into a CUDA graph whose
-branches run on several streams (C ABI: ``spd_ensemble_*``), so one graph
-launch advances the whole ensemble.  ``autotune`` picks the number of
-streams and the cells per block of the predictor's fused kernel by timing
-real ensemble steps.  Every instance produces the same bits as stepping it
-alone.
+different grid sizes together, each with its own CFL dt, in one of two
+forms (C ABI: ``spd_ensemble_*``):
+
+* ``packed=True``: every stage of the step (CFL reduction, predictor
+  kernels, FV update, trouble detection, fallback) is ONE launch over all
+  instances; a per-instance block-offset table maps each thread block to its
+  instance and to its block within that instance.  A whole ensemble step is
+  ~100 launches, captured in one CUDA graph.
+* ``packed=False``: the per-instance step sequences are recorded into one
+  CUDA graph whose branches run on ``nstreams`` streams.
+
+``autotune`` picks the form, the number of streams and the cells per block
+of the predictor's fused kernel by timing real ensemble steps.  Every
+instance produces the same bits as stepping it alone.
 """
 from __future__ import annotations
 
@@ -19,7 +26,7 @@ from . import _lib
 
 
 class SDADER_Ensemble:
-    def __init__(self, simulators, nstreams: int = 8, steps_per_launch: int = 1):
+    def __init__(self, simulators, nstreams: int = 8, steps_per_launch: int = 1, packed: bool = False):
         self.sims = list(simulators)
         if not self.sims:
             raise ValueError("empty ensemble")
@@ -27,6 +34,7 @@ class SDADER_Ensemble:
         self._declare()
         self.nstreams = nstreams
         self.steps_per_launch = steps_per_launch
+        self.packed = packed
         self.tuning = None
         self._ens = None
         self._build()
@@ -36,6 +44,9 @@ class SDADER_Ensemble:
         vp = ctypes.c_void_p
         lib.spd_ensemble_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(vp)]
+        lib.spd_ensemble_create_packed.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int,
+                                                   ctypes.POINTER(vp)]
+        lib.spd_ensemble_graph_nodes.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         lib.spd_ensemble_step.argtypes = [vp, ctypes.c_int]
         lib.spd_ensemble_synchronize.argtypes = [vp]
         lib.spd_ensemble_time.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
@@ -55,10 +66,22 @@ class SDADER_Ensemble:
         self._close()
         arr = (ctypes.c_void_p * len(self.sims))(*[s._ctx.h.value for s in self.sims])
         h = ctypes.c_void_p()
-        rc = self.lib.spd_ensemble_create(arr, len(self.sims), self.nstreams, self.steps_per_launch, ctypes.byref(h))
+        if self.packed:
+            rc = self.lib.spd_ensemble_create_packed(arr, len(self.sims), self.steps_per_launch, ctypes.byref(h))
+        else:
+            rc = self.lib.spd_ensemble_create(arr, len(self.sims), self.nstreams, self.steps_per_launch,
+                                              ctypes.byref(h))
         if rc != 0:
-            raise _lib.SpdError(f"spd_ensemble_create failed with status {rc}")
+            msg = self.lib.spd_ensemble_last_error(None)
+            raise _lib.SpdError(f"ensemble create failed with status {rc}: {msg.decode() if msg else ''}")
         self._ens = h
+
+    def graph_nodes(self) -> int:
+        """Nodes (launches, zero-fills, stream joins) of one ensemble step's
+        CUDA graph."""
+        n = ctypes.c_longlong()
+        self._check(self.lib.spd_ensemble_graph_nodes(self._ens, ctypes.byref(n)), "graph_nodes")
+        return n.value
 
     def _close(self):
         if self._ens is not None and self._ens.value:
@@ -102,15 +125,21 @@ class SDADER_Ensemble:
         self._check(self.lib.spd_ensemble_step(self._ens, launches), "step")
         self._sync_times(n_step)
 
-    def autotune(self, streams=(1, 2, 4, 8, 16, 32), cpbs=(16, 32, 64), probe_launches: int = 2):
-        """Time real ensemble steps for every (streams, cells per block)
-        candidate and keep the fastest.  The probe steps advance the
+    def autotune(self, streams=(1, 2, 4, 8, 16, 32), cpbs=(16, 32, 64), probe_launches: int = 2,
+                 packed=(True, False)):
+        """Time real ensemble steps for every candidate -- the packed form
+        and the stream form with each number of streams, at each cells per
+        block -- and keep the fastest.  The probe steps advance the
         instances and count as steps."""
         results = {}
+        forms = [("packed", 0)] if True in packed else []
+        if False in packed:
+            forms += [("streams", ns) for ns in streams]
         for cpb in cpbs:
             self.set_cells_per_block(cpb)
-            for ns in streams:
-                self.nstreams = ns
+            for form, ns in forms:
+                self.packed = form == "packed"
+                self.nstreams = ns or self.nstreams
                 self._build()
                 self._push_times()
                 self._check(self.lib.spd_ensemble_step(self._ens, 1), "warm-up")
@@ -118,15 +147,22 @@ class SDADER_Ensemble:
                 t0 = time.perf_counter()
                 self._check(self.lib.spd_ensemble_step(self._ens, probe_launches), "probe")
                 self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
-                results[(ns, cpb)] = (time.perf_counter() - t0) / probe_launches
+                results[(form, ns, cpb)] = (time.perf_counter() - t0) / probe_launches
                 self._sync_times((1 + probe_launches) * self.steps_per_launch)
         best = min(results, key=results.get)
-        self.nstreams, cpb = best
+        form, ns, cpb = best
+        self.packed = form == "packed"
+        self.nstreams = ns or self.nstreams
         self.set_cells_per_block(cpb)
         self._build()
-        self.tuning = {"streams": best[0], "cells_per_block": best[1],
+
+        def label(k):
+            return f"packed x{k[2]}" if k[0] == "packed" else f"{k[1]} streams x{k[2]}"
+
+        self.tuning = {"form": form, "streams": ns if form == "streams" else None, "cells_per_block": cpb,
                        "seconds_per_step": results[best] / self.steps_per_launch,
-                       "candidates": {f"{k[0]}x{k[1]}": v for k, v in sorted(results.items())}}
+                       "graph_nodes_per_step": self.graph_nodes() // self.steps_per_launch,
+                       "candidates": {label(k): v for k, v in sorted(results.items(), key=lambda kv: kv[1])}}
         return self.tuning
 
     def close(self):

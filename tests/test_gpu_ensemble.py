@@ -44,12 +44,102 @@ def test_ensemble_autotune_keeps_results():
     ens = SDADER_Ensemble(sims)
     tuning = ens.autotune(streams=(1, 2), cpbs=(16, 32), probe_launches=1)
     steps = sims[0].n_step
-    assert steps == 4 * 2  # 4 candidates x (1 warm-up + 1 probe)
+    assert steps == 6 * 2  # (packed, 1 stream, 2 streams) x 2 cpb candidates x (1 warm-up + 1 probe)
+    assert len(tuning["candidates"]) == 6
+    ens.perform_iterations(1)  # the chosen form keeps stepping from the probes' state
+    steps += 1
     for s in ref:
         for _ in range(steps):
             s.compute_dt()
             s.perform_update()
     for a, b in zip(sims, ref):
+        assert a.n_step == steps
         assert np.array_equal(a.dm.U_sp, b.dm.U_sp)
-    assert tuning["streams"] in (1, 2) and tuning["cells_per_block"] in (16, 32)
+    assert tuning["form"] in ("packed", "streams") and tuning["cells_per_block"] in (16, 32)
+    assert tuning["streams"] in ((None,) if tuning["form"] == "packed" else (1, 2))
     ens.close()
+
+
+def _quadrant(n, p=3):
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import four_quadrant
+    return SDADER_Simulator(p=p, N=(n, n), init_fct=four_quadrant, update="FV", FB=True,
+                            riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                            BC=(("gradfree", "gradfree"),) * 2, verbose=False)
+
+
+def _kh_p(n, seed, p):
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import kelvin_helmholtz
+    return SDADER_Simulator(p=p, N=(n, n), init_fct=kelvin_helmholtz(n, seed=seed), update="FV", FB=True,
+                            riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                            BC=(("periodic", "periodic"),) * 2, verbose=False)
+
+
+def _solo_steps(sims, steps):
+    for s in sims:
+        for _ in range(steps):
+            s.compute_dt()
+            s.perform_update()
+
+
+def _assert_same(ens_sims, solo, steps):
+    for a, b in zip(ens_sims, solo):
+        assert a.n_step == b.n_step == steps
+        assert a.time == b.time
+        assert np.array_equal(a.dm.U_sp, b.dm.U_sp)
+        assert np.array_equal(a.dm.U_cv, b.dm.U_cv)
+        assert np.array_equal(a.dm.W_cv, b.dm.W_cv)
+        assert np.array_equal(a.dm.troubles, b.dm.troubles)
+        assert a.dm.dt == b.dm.dt
+
+
+@pytest.mark.parametrize("steps_per_launch", [1, 2])
+def test_packed_ensemble_matches_individual_runs(steps_per_launch):
+    """One launch per stage over all instances (block-offset table): uneven
+    sides, periodic and transmissive boundaries, per-instance dt."""
+    from spd_gb300 import SDADER_Ensemble
+    sides = [16, 24, 8, 32, 16]
+    make = [lambda i=i, n=n: _kh(n, seed=i) for i, n in enumerate(sides)] + [lambda: _quadrant(16)]
+    ens_sims = [m() for m in make]
+    solo = [m() for m in make]
+    ens = SDADER_Ensemble(ens_sims, packed=True, steps_per_launch=steps_per_launch)
+    nodes = ens.graph_nodes()
+    ens.perform_iterations(4)
+    _solo_steps(solo, 4)
+    _assert_same(ens_sims, solo, 4)
+    assert len({round(s.time, 15) for s in ens_sims}) > 1  # per-instance dt
+    # the packed graph has one node per stage, however many instances
+    single = SDADER_Ensemble([make[0]()], packed=True, steps_per_launch=steps_per_launch)
+    assert nodes == single.graph_nodes()
+    single.close()
+    ens.close()
+
+
+def test_packed_ensemble_odd_substeps():
+    """p = 2: three FV substeps per step, so the buffer roles alternate
+    between steps; several graph replays in a row."""
+    from spd_gb300 import SDADER_Ensemble
+    sides = [12, 20, 8]
+    ens_sims = [_kh_p(n, 30 + i, 2) for i, n in enumerate(sides)]
+    solo = [_kh_p(n, 30 + i, 2) for i, n in enumerate(sides)]
+    ens = SDADER_Ensemble(ens_sims, packed=True)
+    ens.perform_iterations(3)
+    ens.perform_iterations(2)
+    _solo_steps(solo, 5)
+    _assert_same(ens_sims, solo, 5)
+    ens.close()
+
+
+def test_packed_ensemble_rejects_mixed_options():
+    from spd_gb300 import SDADER_Ensemble
+    from spd_gb300._lib import SpdError
+    with pytest.raises(SpdError, match="degree"):
+        SDADER_Ensemble([_kh_p(8, 1, 3), _kh_p(8, 2, 2)], packed=True)
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import kelvin_helmholtz
+    no_fb = SDADER_Simulator(p=3, N=(8, 8), init_fct=kelvin_helmholtz(8, seed=3), update="FV", FB=False,
+                             riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                             BC=(("periodic", "periodic"),) * 2, verbose=False)
+    with pytest.raises(SpdError, match="differ"):
+        SDADER_Ensemble([_kh(8, seed=4), no_fb], packed=True)
