@@ -509,8 +509,13 @@ def ensemble_arm(args):
             s.perform_update()
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
-    ens = SDADER_Ensemble(sims)
-    tuning = ens.autotune(streams=(1, 4, 16), cpbs=(32, 64), probe_launches=1)
+    if args.ensemble_form == "auto":
+        ens = SDADER_Ensemble(sims)
+        tuning = ens.autotune(streams=(1, 4, 16), cpbs=(32, 64), probe_launches=1)
+    else:
+        ens = SDADER_Ensemble(sims, nstreams=16, packed=args.ensemble_form == "packed")
+        tuning = {"form": args.ensemble_form, "streams": None if args.ensemble_form == "packed" else 16,
+                  "cells_per_block": ens.cells_per_block()[0][0], "graph_nodes_per_step": ens.graph_nodes()}
     ens.perform_iterations(args.warmup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -717,6 +722,8 @@ def main():
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=64, help="ensemble size (kh_ensemble)")
+    ap.add_argument("--ensemble-form", default="auto", choices=["auto", "packed", "streams"],
+                    help="batched form (kh_ensemble): autotuned, or fixed without tuning")
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per direction (a smaller case of the workload, for profiling)")
     ap.add_argument("--adj-steps", type=int, default=200, help="time steps of the differentiated run (kh_adjoint)")

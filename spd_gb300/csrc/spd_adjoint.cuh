@@ -50,8 +50,9 @@ __global__ void k_adj_interior(Ops op, Geo g, int mode, int Teff, const double* 
 #pragma unroll
       for (int f = 0; f < k::nf; ++f) Fla[v][f] = Ffa[((((long long)v * g.T + t) * k::NJ + j) * k::nf + f) * nc + c];
   } else {
-    // derivative transpose: val = (sum_f dfp_to_sp[so][f] F[f]) / h
-    const double rh = 1.0 / g.h[d];
+    // derivative transpose: val = (sum_f dfp_to_sp[so][f] F[f]) / h; rh is
+    // the correctly rounded 1/h the host stores for every active direction
+    const double rh = g.inv_h[d];
 #pragma unroll
     for (int v = 0; v < k::V; ++v) {
 #pragma unroll
@@ -470,15 +471,17 @@ __global__ void k_adj_faces(Geo g, FvGeo fg, int d, const double* __restrict__ d
   for (int v = 0; v < V; ++v) {
     double Fa = 0.0;
     int q[3] = {f[0], f[1], f[2]};
+    // quotients by the subcell widths from their correctly rounded
+    // reciprocals (div_rcp: the IEEE quotient's bits in 3 FP64 operations)
     if (f[d] >= 1) {  // right face of subcell f-1
       q[d] = f[d] - 1;
       const long long qi = q[0] + (long long)g.X[0] * (q[1] + (long long)g.X[1] * q[2]);
-      Fa += -dti * Unew_a[(long long)v * g.Nq + qi] / fg.dx[d][q[d]];
+      Fa += div_rcp(-dti * Unew_a[(long long)v * g.Nq + qi], fg.dx[d][q[d]], fg.rdx[d][q[d]]);
     }
     if (f[d] < Xd) {  // left face of subcell f
       q[d] = f[d];
       const long long qi = q[0] + (long long)g.X[0] * (q[1] + (long long)g.X[1] * q[2]);
-      Fa += dti * Unew_a[(long long)v * g.Nq + qi] / fg.dx[d][q[d]];
+      Fa += div_rcp(dti * Unew_a[(long long)v * g.Nq + qi], fg.dx[d][q[d]], fg.rdx[d][q[d]]);
     }
     double ho = Fa, fbv = 0.0;
     if (use_fb) {
@@ -594,15 +597,26 @@ SPD_FN void predictor_vjp(const double* W, const double (*dMh)[D + 2], double dt
 // reconstructed states, FA[side][v][face] (side 0 = left state).  The
 // states are the recorded forward's predictions and slope terms
 // (Mpred [v][e], S [dir][v][e]; valid on the cells of used faces).
+//
+// The used faces and the cells next to them are compacted into index lists
+// first (warp ballot): an FP64 warp instruction costs the same with 1 or 32
+// active lanes, so the VJPs run on full warps over the lists.
 template <int D>
-__global__ void k_adj_muscl_riemann(Geo g, int d, int solver, int godunov, const double* __restrict__ aff,
-                                    const double* __restrict__ Mpred, const double* __restrict__ S,
-                                    const double* __restrict__ Fba, double* __restrict__ FA) {
-  constexpr int V = D + 2;
+__global__ void k_adj_used_faces(Geo g, int d, int godunov, const double* __restrict__ aff,
+                                 long long* __restrict__ list, unsigned long long* __restrict__ count) {
   const long long nf = n_faces(g, d);
   const long long fidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (fidx >= nf) return;
-  if (!(godunov || aff[fidx] != 0.0)) return;
+  const bool used = fidx < nf && (godunov || aff[fidx] != 0.0);
+  warp_append(used, fidx, list, count);
+}
+
+template <int D>
+__device__ __forceinline__ void adj_muscl_riemann_face(const Geo& g, int d, int solver, long long fidx,
+                                                       const double* __restrict__ Mpred,
+                                                       const double* __restrict__ S, const double* __restrict__ Fba,
+                                                       double* __restrict__ FA) {
+  constexpr int V = D + 2;
+  const long long nf = n_faces(g, d);
   const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
   int f[3];
   f[0] = (int)(fidx % FX);
@@ -629,20 +643,64 @@ __global__ void k_adj_muscl_riemann(Geo g, int d, int solver, int godunov, const
   }
 }
 
-// Phase 2, one thread per extended cell e: gathers (in a fixed order) the
+template <int D>
+__global__ void k_adj_muscl_riemann(Geo g, int d, int solver, const long long* __restrict__ list,
+                                    const unsigned long long* __restrict__ count, const double* __restrict__ Mpred,
+                                    const double* __restrict__ S, const double* __restrict__ Fba,
+                                    double* __restrict__ FA) {
+  const unsigned long long cnt = *count;
+  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)gridDim.x * blockDim.x)
+    adj_muscl_riemann_face<D>(g, d, solver, list[idx], Mpred, S, Fba, FA);
+}
+
+// whether extended cell e borders a used face (its state and slopes fed a
+// fallback flux)
+template <int D>
+__device__ __forceinline__ bool borders_used_face(const Geo& g, int godunov, const double* const* AF, long long e) {
+  int ec[3];
+  e_coords(g, e, ec[0], ec[1], ec[2]);
+  for (int dd = 0; dd < D; ++dd) {
+    bool inside = true;
+    int fc[3] = {0, 0, 0};
+    for (int o = 0; o < D; ++o) {
+      if (o == dd) continue;
+      fc[o] = ec[o] - NGH;
+      inside = inside && fc[o] >= 0 && fc[o] < g.X[o];
+    }
+    if (!inside) continue;
+    for (int k = 0; k < 2; ++k) {
+      fc[dd] = ec[dd] - 1 - k;
+      if (fc[dd] < 0 || fc[dd] > g.X[dd]) continue;
+      if (godunov || AF[dd][face_id(g, dd, fc[0], fc[1], fc[2])] != 0.0) return true;
+    }
+  }
+  return false;
+}
+
+template <int D>
+__global__ void k_adj_used_cells(Geo g, int godunov, const double* aff0, const double* aff1, const double* aff2,
+                                 long long* __restrict__ list, unsigned long long* __restrict__ count) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double* AF[3] = {aff0, aff1, aff2};
+  const bool used = e < g.Nqe && borders_used_face<D>(g, godunov, AF, e);
+  warp_append(used, e, list, count);
+}
+
+// Phase 2, one thread per listed extended cell e (the cells bordering a
+// used face; W_a and LA are zero elsewhere): gathers (in a fixed order) the
 // adjoints of its predicted state and slopes from the used faces it
 // borders, takes them back through the prediction and the limiter, writes
 // W_a(e) = the part that lands on W(e) itself and LA[dd][0|1][v](e) =
 // SL_a / hl, SR_a / hr (the parts that land on W(e - st) and W(e + st)).
 template <int D>
-__global__ void k_adj_muscl_cells(Geo g, FvGeo fg, int limiter, int godunov, const double* __restrict__ dt_ptr,
-                                  double w_i, const double* aff0, const double* aff1, const double* aff2,
-                                  const double* FA0, const double* FA1, const double* FA2,
-                                  const double* __restrict__ W_ext, double* __restrict__ W_a,
-                                  double* __restrict__ LA) {
+__device__ __forceinline__ void adj_muscl_cell(const Geo& g, const FvGeo& fg, int limiter, int godunov,
+                                               const double* __restrict__ dt_ptr, double w_i, const double* aff0,
+                                               const double* aff1, const double* aff2, const double* FA0,
+                                               const double* FA1, const double* FA2,
+                                               const double* __restrict__ W_ext, long long e,
+                                               double* __restrict__ W_a, double* __restrict__ LA) {
   constexpr int V = D + 2, NT = V * (1 + D);
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= g.Nqe) return;
   const double* AF[3] = {aff0, aff1, aff2};
   const double* FA[3] = {FA0, FA1, FA2};
   int ec[3];
@@ -709,6 +767,20 @@ __global__ void k_adj_muscl_cells(Geo g, FvGeo fg, int limiter, int godunov, con
     }
   }
   for (int v = 0; v < V; ++v) W_a[(long long)v * g.Nqe + e] = own[v];
+}
+
+template <int D>
+__global__ void k_adj_muscl_cells(Geo g, FvGeo fg, int limiter, int godunov, const double* __restrict__ dt_ptr,
+                                  double w_i, const double* aff0, const double* aff1, const double* aff2,
+                                  const double* FA0, const double* FA1, const double* FA2,
+                                  const double* __restrict__ W_ext, const long long* __restrict__ list,
+                                  const unsigned long long* __restrict__ count, double* __restrict__ W_a,
+                                  double* __restrict__ LA) {
+  const unsigned long long cnt = *count;
+  for (unsigned long long idx = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
+       idx += (unsigned long long)gridDim.x * blockDim.x)
+    adj_muscl_cell<D>(g, fg, limiter, godunov, dt_ptr, w_i, aff0, aff1, aff2, FA0, FA1, FA2, W_ext, list[idx], W_a,
+                      LA);
 }
 
 // Phase 3: W_a(e) += sum over directions of -SL_a/hl of e+st and +SR_a/hr

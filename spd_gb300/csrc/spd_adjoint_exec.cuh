@@ -114,22 +114,46 @@ int adjoint_vjp(spd_ctx* C) {
                                                                 nullptr);
           CKL();
         }
+        // the used faces and the cells bordering them, compacted into the
+        // forward step's scratch lists (same stream, never live at once)
         const double* affd[3] = {nullptr, nullptr, nullptr};
         off = 0;
         for (int d = 0; d < D; ++d) {
           affd[d] = C->hist_aff + (size_t)i * per + off;
           off += (size_t)nface[d];
-          ProfScope ps_(C, "k_adj_muscl_riemann");
-          const double* mp = C->hist_mpred + (size_t)i * (1 + D) * k::V * g.Nqe;
-          k_adj_muscl_riemann<D><<<blocks_for(nface[d], 64), 64, 0, C->stream>>>(
-              g, d, cf.riemann_solver_fv, cf.godunov, affd[d], mp, mp + (size_t)k::V * g.Nqe, C->Fba[d], C->FA[d]);
+        }
+        CK(cudaMemsetAsync(C->counts, 0, sizeof(unsigned long long), C->stream));
+        CK(cudaMemsetAsync(C->counts + 4, 0, D * sizeof(unsigned long long), C->stream));
+        for (int d = 0; d < D; ++d) {
+          ProfScope ps_(C, "k_adj_used_faces");
+          k_adj_used_faces<D><<<blocks_for(nface[d], BS), BS, 0, C->stream>>>(g, d, cf.godunov, affd[d],
+                                                                               C->list_face[d], C->counts + 4 + d);
           CKL();
         }
         {
+          ProfScope ps_(C, "k_adj_used_cells");
+          k_adj_used_cells<D><<<blocks_for(g.Nqe, BS), BS, 0, C->stream>>>(g, cf.godunov, affd[0], affd[1], affd[2],
+                                                                            C->list_cell, C->counts);
+        }
+        CKL();
+        for (int d = 0; d < D; ++d) {
+          ProfScope ps_(C, "k_adj_muscl_riemann");
+          const double* mp = C->hist_mpred + (size_t)i * (1 + D) * k::V * g.Nqe;
+          const unsigned nb = (unsigned)std::min<long long>(PERSIST_BLOCKS, blocks_for(nface[d], 64));
+          k_adj_muscl_riemann<D><<<nb, 64, 0, C->stream>>>(g, d, cf.riemann_solver_fv, C->list_face[d],
+                                                           C->counts + 4 + d, mp, mp + (size_t)k::V * g.Nqe,
+                                                           C->Fba[d], C->FA[d]);
+          CKL();
+        }
+        // W_a and LA are zero on the cells that border no used face
+        CK(cudaMemsetAsync(C->W_a, 0, sizeof(double) * k::V * g.Nqe, C->stream));
+        CK(cudaMemsetAsync(C->LA, 0, sizeof(double) * 2 * D * k::V * g.Nqe, C->stream));
+        {
           ProfScope ps_(C, "k_adj_muscl_cells");
-          k_adj_muscl_cells<D><<<blocks_for(g.Nqe, 64), 64, 0, C->stream>>>(
-              g, C->fvg, cf.slope_limiter, cf.godunov, C->hist_dt, w_i, affd[0], affd[1], affd[2], C->FA[0],
-              C->FA[1], C->FA[2], C->W_ext, C->W_a, C->LA);
+          const unsigned nb = (unsigned)std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nqe, 64));
+          k_adj_muscl_cells<D><<<nb, 64, 0, C->stream>>>(g, C->fvg, cf.slope_limiter, cf.godunov, C->hist_dt, w_i,
+                                                         affd[0], affd[1], affd[2], C->FA[0], C->FA[1], C->FA[2],
+                                                         C->W_ext, C->list_cell, C->counts, C->W_a, C->LA);
         }
         CKL();
         {

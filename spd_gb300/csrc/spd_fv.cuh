@@ -59,6 +59,17 @@ __device__ __forceinline__ double from_order_key(long long k) {
 __device__ __forceinline__ bool is_nan_bits(double x) {
   return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
+// NumPy maximum (a if a >= b or a is NaN, else b) on the integer pipes
+__device__ __forceinline__ double np_max_key(double a, double b) {
+  if (is_nan_bits(a)) return a;
+  if (is_nan_bits(b)) return b;
+  return order_key(a) >= order_key(b) ? a : b;
+}
+// x > 0 on the bits (false for zeros, negatives and NaN)
+__device__ __forceinline__ bool gt0_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
 
 // dUdt of one subcell from the face fluxes (src/fv_simulator.py:189-205)
 template <int D>
@@ -229,7 +240,11 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, double tol, int 
         }
       }
       const double wn = ext_new[(long long)v * g.Nqe + e];
-      const bool pt = nan || !(wn >= mn) || !(wn <= mx);
+      // !(wn >= mn) || !(wn <= mx) on the integer keys: true when any of the
+      // three is NaN, else the ordered comparison (the keys equate -0, +0)
+      const long long kw = order_key(wn);
+      const bool pt = nan || is_nan_bits(wn) || is_nan_bits(mn) || is_nan_bits(mx) || kw < order_key(mn) ||
+                      kw > order_key(mx);
       m |= (pt ? 1u : 0u) << v;
     }
     mask[q] = (unsigned char)m;
@@ -413,13 +428,13 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __
     for (int s = -1; s <= 1; s += 2) {
       int cc[3] = {c[0], c[1], c[2]};
       cc[d] += s;
-      if (inb(d, cc[d])) th = np_max(0.75 * at(cc[0], cc[1], cc[2]), th);
+      if (inb(d, cc[d])) th = np_max_key(0.75 * at(cc[0], cc[1], cc[2]), th);
     }
   }
   if (D == 2) {
     for (int sy = -1; sy <= 1; sy += 2)
       for (int sx = -1; sx <= 1; sx += 2)
-        if (inb(0, c[0] + sx) && inb(1, c[1] + sy)) th = np_max(0.5 * at(c[0] + sx, c[1] + sy, 0), th);
+        if (inb(0, c[0] + sx) && inb(1, c[1] + sy)) th = np_max_key(0.5 * at(c[0] + sx, c[1] + sy, 0), th);
   } else if (D == 3) {
     // (axis pair, offsets) per (i, idim); axes listed as (first, second)
     // cut axis; offset 0 with range e < last (cut a) or e >= 1 (cut b)
@@ -439,7 +454,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __
           if (kinds[i][k2] == 1 && c[ax] < 1) ok = false;
           cc[ax] += offs[i][k2];
         }
-        if (ok) th = np_max(0.5 * at(cc[0], cc[1], cc[2]), th);
+        if (ok) th = np_max_key(0.5 * at(cc[0], cc[1], cc[2]), th);
       }
     }
     // third neighbours: offsets on (z, y, x)
@@ -448,7 +463,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __
       const int oz = t3[i][0], oy = t3[i][1], ox = t3[i][2];
       const bool ok = (oz > 0 ? c[2] < g.Xe[2] - 1 : c[2] >= 1) && (oy > 0 ? c[1] < g.Xe[1] - 1 : c[1] >= 1) &&
                       (ox > 0 ? c[0] < g.Xe[0] - 1 : c[0] >= 1);
-      if (ok) th = np_max(0.375 * at(c[0] + ox, c[1] + oy, c[2] + oz), th);
+      if (ok) th = np_max_key(0.375 * at(c[0] + ox, c[1] + oy, c[2] + oz), th);
     }
   }
   out[e] = th;
@@ -473,14 +488,14 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, const dou
   const int last = g.Xe[d] - 1;
   auto th_a = [&](int k, long long ek) {  // after the first sweep
     const double t = in[ek];
-    if (k < last) return np_max(0.25 * ((in[ek + st] > 0) ? 1.0 : 0.0), t);
+    if (k < last) return np_max_key(gt0_key(in[ek + st]) ? 0.25 : 0.0, t);
     return t;
   };
   const int k = c[d];
   const double a0 = th_a(k, e);
   if (k >= 1) {
     const double am = th_a(k - 1, e - st);
-    out[e] = np_max(0.25 * ((am > 0) ? 1.0 : 0.0), a0);
+    out[e] = np_max_key(gt0_key(am) ? 0.25 : 0.0, a0);
   } else {
     out[e] = a0;
   }
@@ -523,7 +538,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int godun
     const long long i2 = e2[0] + (long long)g.Xe[0] * (e2[1] + (long long)g.Xe[1] * e2[2]);
     double a;
     if (theta) {
-      a = np_max(theta[i1], theta[i2]);
+      a = np_max_key(theta[i1], theta[i2]);
       aff[fidx] = a;
     } else {
       a = aff[fidx];
@@ -569,6 +584,20 @@ __global__ void k_affected(Geo g, int d, int godunov, const double* __restrict__
 
 // compaction of marked indices by warp ballot: writes the marked indices
 // into list and their count into *count.
+// Appends ``value`` of every lane with ``keep`` to list (order within the
+// list unspecified), one atomic per warp.  All 32 lanes of the warp must
+// call it.
+__device__ __forceinline__ void warp_append(bool keep, long long value, long long* __restrict__ list,
+                                            unsigned long long* __restrict__ count) {
+  const unsigned b = __ballot_sync(0xffffffffu, keep);
+  if (b == 0) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) list[base + __popc(b & ((1u << lane) - 1u))] = value;
+}
+
 struct Compact {
   static __device__ __forceinline__ void run(Blk B, long long total, const unsigned char* __restrict__ mark,
                                              long long* __restrict__ list, unsigned long long* __restrict__ count) {

@@ -163,20 +163,20 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
     const double Pstar = low_mach ? div_rcp(rcR * WL[P_] + rcL * WR[P_] + phi * rcL * rcR * (vL - vR), den, rden)
                                   : div_rcp(rcR * WL[P_] + rcL * WR[P_] + rcL * rcR * (vL - vR), den, rden);
     int region;
-    double r, vg, Pg, e, dd = 1.0;
+    double r, vg, Pg, e, dd = 1.0, rdd = 1.0;
     if (sL > 0.0) {
       region = 0; r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
-    } else if (vstar > 0.0) {
-      region = 1; dd = sL - vstar;
-      const double rd = 1.0 / dd;
-      r = div_rcp(WL[0] * (sL - vL), dd, rd);
-      e = div_rcp((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar, dd, rd);
-      vg = vstar; Pg = Pstar;
-    } else if (sR > 0.0) {
-      region = 2; dd = sR - vstar;
-      const double rd = 1.0 / dd;
-      r = div_rcp(WR[0] * (sR - vR), dd, rd);
-      e = div_rcp((sR - vR) * UR[P_] - WR[P_] * vR + Pstar * vstar, dd, rd);
+    } else if (vstar > 0.0 || sR > 0.0) {
+      // left (region 1) and right (region 2) star states: one path with
+      // per-lane operands (both sides of a warp evaluate it once)
+      const bool lft = vstar > 0.0;
+      region = lft ? 1 : 2;
+      const double s = lft ? sL : sR, v = lft ? vL : vR;
+      const double w0 = lft ? WL[0] : WR[0], wP = lft ? WL[P_] : WR[P_], uP = lft ? UL[P_] : UR[P_];
+      dd = s - vstar;
+      rdd = 1.0 / dd;
+      r = div_rcp(w0 * (s - v), dd, rdd);
+      e = div_rcp((s - v) * uP - wP * v + Pstar * vstar, dd, rdd);
       vg = vstar; Pg = Pstar;
     } else {
       region = 3; r = WR[0]; vg = vR; Pg = WR[P_]; e = UR[P_];
@@ -211,8 +211,7 @@ SPD_FN void riemann_vjp_rev(int solver, const double* ML, const double* MR, cons
       const double sK = isL ? sL : sR;
       const double EK = isL ? UL[P_] : UR[P_];
       const double PK = isL ? WL[P_] : WR[P_];
-      // r = rho (sK - vK) / dd, dd = sK - vstar
-      const double rdd = 1.0 / dd;
+      // r = rho (sK - vK) / dd, dd = sK - vstar (rdd = 1 / dd from above)
       double rho_a = ra * (sK - vK) * rdd;
       double sK_a = (ra * rho - ra * r) * rdd;
       double vK_a = -ra * rho * rdd;
