@@ -9,6 +9,8 @@ operation sequence, so the matrices are the same bits on the same platform.
 """
 from __future__ import annotations
 
+import concurrent.futures
+import os
 from typing import Callable, Tuple
 
 import numpy as np
@@ -78,9 +80,11 @@ def ader_matrix(x_time: np.ndarray, w_time: np.ndarray, dt: float) -> np.ndarray
     return ltm[None, :] * ltm[:, None] - lpm.T * w_time[None, :]
 
 
-def quadrature_mean(mesh: np.ndarray, fct: Callable, d: int, v: int, light: bool = True) -> np.ndarray:
-    """Cell means of fct(x, v) over the control volumes of ``mesh`` with a
-    tensor Gauss-Legendre rule (src/polynomials.py:124-148)."""
+def quadrature_points(mesh: np.ndarray, d: int, light: bool = True):
+    """Tensor Gauss-Legendre points of every control volume of ``mesh`` and
+    the 1D weights (src/polynomials.py:124-148).  The points do not depend
+    on the variable, so a caller sampling several variables builds them
+    once.  The returned point array is read-only."""
     nq = 2 if light else max(mesh.shape[-d:]) - 1
     x, w = gauss_legendre_quadrature(0.0, 1.0, nq)
     pts = mesh[(Ellipsis,) + (slice(-1),) * d + (np.newaxis,) * d]
@@ -89,6 +93,16 @@ def quadrature_mean(mesh: np.ndarray, fct: Callable, d: int, v: int, light: bool
         edges = mesh[(Ellipsis,) + (slice(-1),) * i + (slice(None),) + (slice(-1),) * (d - i - 1)]
         pts += (np.diff(edges, axis=(i - d))[(Ellipsis,) + (np.newaxis,) * d]
                 * x[(np.newaxis,) * len(mesh.shape) + (np.newaxis,) * i + (slice(None),) + (np.newaxis,) * (d - i - 1)])
+    pts.setflags(write=False)
+    return pts, w
+
+
+def quadrature_mean(mesh: np.ndarray, fct: Callable, d: int, v: int, light: bool = True,
+                    points=None) -> np.ndarray:
+    """Cell means of fct(x, v) over the control volumes of ``mesh`` with a
+    tensor Gauss-Legendre rule (src/polynomials.py:124-148).  ``points`` is
+    the result of quadrature_points(mesh, d, light) when already built."""
+    pts, w = points if points is not None else quadrature_points(mesh, d, light)
     args = [fct(pts, v), (Ellipsis,) + tuple(range(d))]
     for i in range(d):
         args.extend([w, (i,)])
@@ -122,3 +136,29 @@ def transform_full(B: np.ndarray, A: np.ndarray, ndim: int) -> np.ndarray:
     if ndim == 2:
         return np.einsum("jm,il,uyxml->uyxji", A, A, B)
     return np.einsum("il,uxl->uxi", A, B)
+
+
+def transform_full_threaded(B: np.ndarray, A: np.ndarray, ndim: int, min_cells: int = 1 << 16,
+                            workers: int | None = None) -> np.ndarray:
+    """transform_full of a C-contiguous SD-layout array on several host
+    threads: slabs of whole (variable, outermost cell row) blocks, each the
+    same einsum on its slab (einsum releases the GIL).  Every output
+    element is the same sum over its own cell's points as in one einsum of
+    the whole array (bit-identical; checked in the CPU tests).  Arrays of
+    fewer than ``min_cells`` cells take the single call."""
+    ncells = int(np.prod(B.shape[1:1 + ndim]))
+    workers = workers or min(16, os.cpu_count() or 1)
+    if ncells < min_cells or workers < 2 or not B.flags.c_contiguous:
+        return transform_full(B, A, ndim)
+    flat = B.reshape((B.shape[0] * B.shape[1],) + B.shape[2:])
+    out = np.empty_like(flat)
+    bounds = np.linspace(0, flat.shape[0], min(workers * 4, flat.shape[0]) + 1).astype(int)
+
+    def one(k):
+        lo, hi = bounds[k], bounds[k + 1]
+        if hi > lo:
+            out[lo:hi] = transform_full(flat[lo:hi][:, None], A, ndim)[:, 0]
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(one, range(len(bounds) - 1)))
+    return out.reshape(B.shape)

@@ -23,8 +23,8 @@ import numpy as np
 from . import _lib
 from .initial_conditions import sine_wave
 from .polynomials import (ader_matrix, flux_points, gauss_legendre_quadrature, intfromsol_matrix,
-                          lagrange_matrix, lagrangeprime_matrix, quadrature_mean, solution_points,
-                          transform_axis, transform_full)
+                          lagrange_matrix, lagrangeprime_matrix, quadrature_mean, quadrature_points,
+                          solution_points, transform_axis, transform_full, transform_full_threaded)
 
 DIMS = ("x", "y", "z")
 
@@ -88,11 +88,14 @@ def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1):
     vels = np.arange(ndim) + 1
     mesh = mesh_cv(ndim, N, p, lims, Nghe, ops["x_fp"])
     W_gh = np.ndarray((nvar,) + tuple(N[i] + 2 * Nghe for i in range(ndim))[::-1] + (p + 1,) * ndim)
+    # the quadrature points are the same for every variable: built once
+    points = quadrature_points(mesh, ndim)
     for var in range(nvar):
-        W_gh[var] = quadrature_mean(mesh, init_fct, ndim, var)
+        W_gh[var] = quadrature_mean(mesh, init_fct, ndim, var, points=points)
+    del points
     W_init_cv = W_gh[(slice(None),) + (slice(Nghe, -Nghe),) * ndim + (Ellipsis,)]
     W_cv = W_init_cv.copy()
-    W_sp = transform_full(W_cv, ops["cv_to_sp"], ndim)
+    W_sp = transform_full_threaded(W_cv, ops["cv_to_sp"], ndim)
     U_sp = _conservatives(W_sp, vels, ndim + 1, gamma)
     U_cv = _conservatives(W_cv, vels, ndim + 1, gamma)
     return W_gh, W_init_cv, W_sp, U_sp, U_cv

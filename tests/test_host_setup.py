@@ -81,3 +81,30 @@ def test_unsupported_options_raise():
         SDADER_Simulator(N=(4,), slope_limiter="superbee")
     with pytest.raises(TypeError):
         SDADER_Simulator(N=(4,), BC=(("open", "open"),))
+
+
+@pytest.mark.parametrize("ndim,p,N", [(1, 3, 3000), (2, 3, 40), (2, 2, 96), (3, 2, 20), (3, 4, 12)])
+def test_threaded_transform_full_is_bitwise(ndim, p, N):
+    """transform_full on thread slabs gives the same bits as one einsum."""
+    from spd_gb300.polynomials import transform_full, transform_full_threaded
+    rng = np.random.default_rng(ndim * 100 + p)
+    shape = (ndim + 2,) + (N,) * ndim + (p + 1,) * ndim
+    B = rng.standard_normal(shape) * 10.0 ** rng.uniform(-6, 6, shape)
+    A = SDADER_Simulator.build_operators(p, p)["cv_to_sp"]
+    assert np.array_equal(transform_full(B, A, ndim), transform_full_threaded(B, A, ndim, min_cells=1, workers=4))
+
+
+def test_initial_state_builds_quadrature_points_once():
+    """initial_state (points built once, threaded transform) equals the
+    per-variable quadrature and single-call transform of the reference."""
+    from spd_gb300.initial_conditions import kelvin_helmholtz
+    from spd_gb300.polynomials import quadrature_mean, transform_full
+    from spd_gb300.simulator import mesh_cv
+    N, p = [300, 260], 3
+    ops = SDADER_Simulator.build_operators(p, p)
+    fct = kelvin_helmholtz(300, seed=5)
+    W_gh, W_init_cv, W_sp, U_sp, U_cv = initial_state(2, N, p, [(0.0, 1.0), (0.0, 1.0)], fct, ops, 1.4)
+    mesh = mesh_cv(2, N, p, [(0.0, 1.0), (0.0, 1.0)], 1, ops["x_fp"])
+    for var in range(4):
+        assert np.array_equal(W_gh[var], quadrature_mean(mesh, fct, 2, var))
+    assert np.array_equal(W_sp, transform_full(W_init_cv.copy(), ops["cv_to_sp"], 2))
