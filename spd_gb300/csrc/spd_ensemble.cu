@@ -60,6 +60,29 @@ int efail(spd_ensemble* E, int code, const std::string& msg) {
     if (e_ != cudaSuccess) return efail(E, SPD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// Host-side buffer roles of the contexts.  Recording or capturing a step
+// leaves them as after one step although no step has run yet; the guard
+// puts back the roles of before on every exit of the create function, and
+// spd_ensemble_step applies the roles of after once a step has run.
+struct RolesGuard {
+  std::vector<spd_ctx*> cs;
+  std::vector<double*> pre;
+  explicit RolesGuard(const std::vector<spd_ctx*>& c) : cs(c) {
+    for (spd_ctx* C : cs) {
+      pre.push_back(C->U_cv);
+      pre.push_back(C->U_new);
+      pre.push_back(C->theta_final);
+    }
+  }
+  ~RolesGuard() {
+    for (size_t i = 0; i < cs.size(); ++i) {
+      cs[i]->U_cv = pre[3 * i];
+      cs[i]->U_new = pre[3 * i + 1];
+      cs[i]->theta_final = pre[3 * i + 2];
+    }
+  }
+};
+
 // one step of one instance on stream s, no host synchronisation
 int enqueue_step(spd_ctx* C, cudaStream_t s) {
   cudaStream_t keep = C->stream;
@@ -118,6 +141,7 @@ int spd_ensemble_create(spd_ctx** ctxs, int n, int nstreams, int steps_per_launc
     lane[i] = best;
     load[best] += E->ctx[i]->geo.Nq;
   }
+  const RolesGuard roles_before(E->ctx);
   ECK(cudaStreamBeginCapture(E->main, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(E->fork, E->main);
   for (int s = 0; s < nstreams; ++s) cudaStreamWaitEvent(E->streams[s], E->fork, 0);
@@ -173,6 +197,7 @@ int spd_ensemble_create_packed(spd_ctx** ctxs, int n, int steps_per_launch, spd_
   // i-th launch of every instance into one batched launch
   E->packed.reset(new spd_batch::BatchRec());
   spd_batch::BatchRec* R = E->packed.get();
+  const RolesGuard roles_before(E->ctx);
   for (int i = 0; i < n && R->err.empty(); ++i) {
     spd_ctx* C = E->ctx[i];
     const bool prof = C->prof;

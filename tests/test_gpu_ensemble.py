@@ -143,3 +143,24 @@ def test_packed_ensemble_rejects_mixed_options():
                              BC=(("periodic", "periodic"),) * 2, verbose=False)
     with pytest.raises(SpdError, match="differ"):
         SDADER_Ensemble([_kh(8, seed=4), no_fb], packed=True)
+
+
+@pytest.mark.parametrize("packed", [True, False])
+def test_ensemble_creation_leaves_state_readable(packed):
+    """Building an ensemble records one step of every instance without
+    running it: the state read back before the first ensemble step is the
+    state before the build (p = 2: an odd number of FV substeps, so a step
+    swaps the roles of the subcell buffers)."""
+    from spd_gb300 import SDADER_Ensemble
+    sims = [_kh_p(n, 40 + i, 2) for i, n in enumerate([8, 16])]
+    for s in sims:  # one plain step so that every buffer holds data
+        s.compute_dt()
+        s.perform_update()
+    before = [(s.dm.U_sp, s.dm.U_cv, s.dm.W_cv, s.dm.theta) for s in sims]
+    ens = SDADER_Ensemble(sims, packed=packed, nstreams=2)
+    for s, (u_sp, u_cv, w_cv, theta) in zip(sims, before):
+        assert np.array_equal(s.dm.U_sp, u_sp)
+        assert np.array_equal(s.dm.U_cv, u_cv)
+        assert np.array_equal(s.dm.W_cv, w_cv)
+        assert np.array_equal(s.dm.theta, theta)
+    ens.close()
