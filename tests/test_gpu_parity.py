@@ -56,22 +56,24 @@ def test_vortex_32_p3_100_steps_bitwise():
     assert not bad, bad
 
 
-def test_quadrant_64_p3_20_steps_bitwise():
+def test_quadrant_64_p3_100_steps_bitwise():
     """Four-quadrant Riemann problem at 64x64 cells (the 512x512 benchmark
-    reduced), transmissive boundaries, HLLC, limiting, 20 steps."""
+    reduced), transmissive boundaries, HLLC, limiting, 100 steps: state,
+    dt and trouble masks bit-identical to the oracle."""
     from spd_gb300.initial_conditions import four_quadrant
-    bad, troubles = _run_vs_oracle(20, p=3, N=(64, 64), init_fct=four_quadrant, update="FV", FB=True,
+    bad, troubles = _run_vs_oracle(100, p=3, N=(64, 64), init_fct=four_quadrant, update="FV", FB=True,
                                    riemann_solver_sd="hllc", riemann_solver_fv="hllc",
                                    BC=(("gradfree", "gradfree"),) * 2)
     assert troubles > 0
     assert not bad, bad
 
 
-def test_sedov_16_p2_10_steps_bitwise():
+def test_sedov_16_p2_100_steps_bitwise():
     """3D Sedov blast at 16^3 cells (the 128^3 benchmark reduced), p=2,
-    reflective walls, HLLC, limiting, 10 steps."""
+    reflective walls, HLLC, limiting, 100 steps: state, dt and trouble
+    masks bit-identical to the oracle."""
     from spd_gb300.initial_conditions import sedov
-    bad, troubles = _run_vs_oracle(10, p=2, N=(16, 16, 16), init_fct=sedov(16), update="FV", FB=True,
+    bad, troubles = _run_vs_oracle(100, p=2, N=(16, 16, 16), init_fct=sedov(16), update="FV", FB=True,
                                    riemann_solver_sd="hllc", riemann_solver_fv="hllc",
                                    BC=(("reflective", "reflective"),) * 3)
     assert troubles > 0
