@@ -5,11 +5,12 @@ counterpart).
 different grid sizes together, each with its own CFL dt, in one of two
 forms (C ABI: ``spd_ensemble_*``):
 
-* ``packed=True``: every stage of the step (CFL reduction, predictor
+* ``packed=True`` (default): every stage of the step (CFL reduction, predictor
   kernels, FV update, trouble detection, fallback) is ONE launch over all
   instances; a per-instance block-offset table maps each thread block to its
   instance and to its block within that instance.  A whole ensemble step is
-  ~100 launches, captured in one CUDA graph.
+  one CUDA graph of ~130 launches (2D, p=3, limiting), however many
+  instances there are.
 * ``packed=False``: the per-instance step sequences are recorded into one
   CUDA graph whose branches run on ``nstreams`` streams.
 
@@ -26,7 +27,7 @@ from . import _lib
 
 
 class SDADER_Ensemble:
-    def __init__(self, simulators, nstreams: int = 8, steps_per_launch: int = 1, packed: bool = False):
+    def __init__(self, simulators, nstreams: int = 8, steps_per_launch: int = 1, packed: bool = True):
         self.sims = list(simulators)
         if not self.sims:
             raise ValueError("empty ensemble")

@@ -20,7 +20,7 @@ def test_ensemble_matches_individual_runs(nstreams):
     sides = [16, 24, 8, 32, 16]
     ens_sims = [_kh(n, seed=i) for i, n in enumerate(sides)]
     solo = [_kh(n, seed=i) for i, n in enumerate(sides)]
-    ens = SDADER_Ensemble(ens_sims, nstreams=nstreams)
+    ens = SDADER_Ensemble(ens_sims, nstreams=nstreams, packed=False)
     ens.perform_iterations(4)
     for s in solo:
         for _ in range(4):
@@ -163,4 +163,31 @@ def test_ensemble_creation_leaves_state_readable(packed):
         assert np.array_equal(s.dm.U_cv, u_cv)
         assert np.array_equal(s.dm.W_cv, w_cv)
         assert np.array_equal(s.dm.theta, theta)
+    ens.close()
+
+
+@pytest.mark.parametrize("ndim", [1, 3])
+def test_packed_ensemble_1d_3d(ndim):
+    """Packed launches in 1D (Sod tubes, p=3) and 3D (Sedov blasts, p=2,
+    reflective and transmissive walls): bit-identical to solo runs."""
+    from spd_gb300 import SDADER_Ensemble, SDADER_Simulator
+    from spd_gb300.initial_conditions import sedov, sod
+
+    def make(n, bc):
+        if ndim == 1:
+            return SDADER_Simulator(p=3, N=(n,), init_fct=sod, update="FV", FB=True,
+                                    riemann_solver_sd="hllc", riemann_solver_fv="hllc", BC=((bc, bc),),
+                                    verbose=False)
+        return SDADER_Simulator(p=2, N=(n, n, n), init_fct=sedov(n), update="FV", FB=True,
+                                riemann_solver_sd="hllc", riemann_solver_fv="hllc", BC=((bc, bc),) * 3,
+                                verbose=False)
+
+    cases = [(64, "gradfree"), (40, "reflective"), (100, "gradfree")] if ndim == 1 else \
+        [(6, "reflective"), (8, "gradfree"), (4, "reflective")]
+    ens_sims = [make(n, bc) for n, bc in cases]
+    solo = [make(n, bc) for n, bc in cases]
+    ens = SDADER_Ensemble(ens_sims, packed=True)
+    ens.perform_iterations(3)
+    _solo_steps(solo, 3)
+    _assert_same(ens_sims, solo, 3)
     ens.close()
