@@ -314,6 +314,19 @@ def whole_job_rate(units_per_rank_step, steps, world, ms):
     return units_per_rank_step * steps * world / (ms / 1e3)
 
 
+def shard_instances(work, world):
+    """Independent ensemble instances split over ``world`` ranks (no
+    collective on the data path): largest first, each to the rank with the
+    least work so far.  Returns the instance indices of every rank."""
+    load = [0] * world
+    shards = [[] for _ in range(world)]
+    for i in sorted(range(len(work)), key=lambda k: (-work[k], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        shards[r].append(i)
+        load[r] += work[i]
+    return [sorted(s) for s in shards]
+
+
 # ---------------------------------------------------------------------------
 # the GPU arm
 # ---------------------------------------------------------------------------
@@ -479,60 +492,83 @@ def ours(args):
 
 
 def ensemble_arm(args):
-    """Batched ensemble vs the plain per-instance loop on the same instances."""
+    """Batched ensemble vs the plain per-instance loop on the same instances.
+    Under torchrun the instances are sharded over the ranks (balanced by
+    DOF, no collective on the data path; strong scaling: the ensemble is
+    fixed); each rank advances its share, the slowest rank's time counts."""
     import numpy as np
     import torch
     from spd_gb300 import SDADER_Ensemble, SDADER_Simulator
     from spd_gb300.initial_conditions import kelvin_helmholtz
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     rng = np.random.default_rng(2026)
     small = args.workload == "kh_ensemble_small"
     choices = [16, 24, 32, 48, 64] if small else [64, 128, 192, 256, 384, 512]
     sides = [int(x) for x in rng.choice(choices, size=args.instances)]
+    mine = shard_instances([n * n for n in sides], world)[rank]
 
     def make(i, n):
         return SDADER_Simulator(p=3, N=(n, n), init_fct=kelvin_helmholtz(n, seed=1000 + i), update="FV", FB=True,
                                 riemann_solver_sd="hllc", riemann_solver_fv="hllc",
                                 BC=(("periodic", "periodic"),) * 2, verbose=False)
 
-    sims = [make(i, n) for i, n in enumerate(sides)]
+    def timed(fn):
+        """fn's wall time on this rank between synchronised starts, max over ranks (s)."""
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return max_over_ranks((time.perf_counter() - t0) * 1e3, dist, "cuda") / 1e3
+
+    sims = [make(i, sides[i]) for i in mine]
     dof = sum(n * n * 16 for n in sides)
-    # plain per-instance loop (compute_dt + perform_update per instance and step)
-    for s in sims:
-        for _ in range(args.warmup):
-            s.compute_dt()
-            s.perform_update()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in sims:
-        for _ in range(args.steps):
-            s.compute_dt()
-            s.perform_update()
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
-    if args.ensemble_form == "auto":
-        ens = SDADER_Ensemble(sims)
-        tuning = ens.autotune(streams=(1, 4, 16), cpbs=(32, 64), probe_launches=1)
-    else:
-        ens = SDADER_Ensemble(sims, nstreams=16, packed=args.ensemble_form == "packed")
-        tuning = {"form": args.ensemble_form, "streams": None if args.ensemble_form == "packed" else 16,
-                  "cells_per_block": ens.cells_per_block()[0][0], "graph_nodes_per_step": ens.graph_nodes()}
-    ens.perform_iterations(args.warmup)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ens.perform_iterations(args.steps)
-    batched_s = time.perf_counter() - t0
+
+    def plain_loop(nsteps):
+        # plain per-instance loop (compute_dt + perform_update per instance and step)
+        for sm in sims:
+            for _ in range(nsteps):
+                sm.compute_dt()
+                sm.perform_update()
+
+    plain_loop(args.warmup)
+    plain_s = timed(lambda: plain_loop(args.steps))
+    ens, tuning = None, None
+    if sims:
+        if args.ensemble_form == "auto":
+            ens = SDADER_Ensemble(sims)
+            tuning = ens.autotune(streams=(1, 4, 16), cpbs=(32, 64), probe_launches=1)
+        else:
+            ens = SDADER_Ensemble(sims, nstreams=16, packed=args.ensemble_form == "packed")
+            tuning = {"form": args.ensemble_form, "streams": None if args.ensemble_form == "packed" else 16,
+                      "cells_per_block": ens.cells_per_block()[0][0], "graph_nodes_per_step": ens.graph_nodes()}
+        ens.perform_iterations(args.warmup)
+    batched_s = timed(lambda: ens.perform_iterations(args.steps) if ens else None)
     plain = dof * args.steps / plain_s
     batched = dof * args.steps / batched_s
-    line = {"metric": METRIC + "; batched/plain speedup", "value": batched, "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_s / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "instances": len(sides), "sides": sides,
-                       "dof_per_ensemble_step": dof},
-            "plain_loop_value": plain, "batched_over_plain": batched / plain, "autotune": tuning}
-    print(json.dumps(line), flush=True)
-    ens.close()
-    for s in sims:
-        s.close()
+    if rank == 0:
+        line = {"metric": METRIC + "; batched/plain speedup", "value": batched, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_s / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOADS[args.workload], "instances": len(sides), "sides": sides,
+                           "dof_per_ensemble_step": dof,
+                           "parallelism": f"instances sharded over {world} GPUs" if world > 1 else "1 GPU"},
+                "plain_loop_value": plain, "batched_over_plain": batched / plain, "autotune": tuning}
+        print(json.dumps(line), flush=True)
+    if ens:
+        ens.close()
+    for sm in sims:
+        sm.close()
+    if dist:
+        dist.destroy_process_group()
 
 
 def adjoint_arm(args):
@@ -732,11 +768,12 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
-    elif args.workload in ("kh_ensemble", "kh_ensemble_small", "kh_adjoint") and int(os.environ.get("RANK", "0")):
-        return  # these workloads run on one GPU: under torchrun only rank 0 runs them
+    elif args.workload == "kh_adjoint" and int(os.environ.get("RANK", "0")):
+        return  # the adjoint workload runs on one GPU: under torchrun only rank 0 runs it
     elif args.workload in ("kh_ensemble", "kh_ensemble_small"):
         from spd_gb300.build import build
-        build()
+        if int(os.environ.get("LOCAL_RANK", "0")) == 0:
+            build()
         if args.workload == "kh_ensemble_small" and args.instances == 64:
             args.instances = 256
         ensemble_arm(args)

@@ -52,3 +52,21 @@ def test_single_process_needs_no_collective():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.max_over_ranks(12.5, None, "cpu") == 12.5
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 8])
+def test_ensemble_instances_shard_over_ranks(world):
+    """Every instance lands on exactly one rank and the per-rank DOF stay
+    within one instance of each other (largest first, least loaded rank)."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    rng = np.random.default_rng(2026)
+    sides = [int(x) for x in rng.choice([64, 128, 192, 256, 384, 512], size=64)]
+    work = [n * n for n in sides]
+    shards = bench.shard_instances(work, world)
+    assert len(shards) == world
+    assert sorted(i for s in shards for i in s) == list(range(len(work)))
+    loads = [sum(work[i] for i in s) for s in shards]
+    assert max(loads) - min(loads) <= max(work)
+    assert bench.shard_instances([5, 1], 4)[2:] == [[], []]  # more ranks than instances: idle ranks
