@@ -242,7 +242,12 @@ __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double
 // ---------------------------------------------------------------------------
 // interior flux points, derivative, Picard update (src/sdader_simulator.py:
 // 148-200) or the final SD update (:202-208) or the flux-point output for
-// the FV update (:288-298).  Block = (CPB cells) x (Teff time nodes).
+// the FV update (:288-298).  Block = (CPB cells) x (rows >= Teff): rows
+// tl < Teff compute the flux derivative of time node tl (Teff = 1 in the
+// first Picard iteration, else T); after the barrier every row writes its
+// share of the outputs (time node t_out = tl, tl + rows, ...), so the first
+// iteration may run with T rows and its single computed node spread over
+// them (CPB a multiple of 32 keeps every warp in one row).
 // mode: 0 = Picard (writes U_ader and next traces), 1 = SD update of U_sp,
 //       2 = write Ffp.
 // ---------------------------------------------------------------------------
@@ -262,7 +267,7 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
   const double* Fi[3] = {Fi0, Fi1, Fi2};
   double* Ffp[3] = {Ffp0, Ffp1, Ffp2};
   const int tu = (Tu == 1) ? 0 : tl;
-  if (active) {
+  if (active && tl < Teff) {
     int cx, cy, cz;
     cell_coords(g, c, cx, cy, cz);
 #pragma unroll
@@ -327,7 +332,7 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
   };
   if (mode == 0) {
     double* tr[3] = {tr0, tr1, tr2};
-    for (int t_out = tl; t_out < g.T; t_out += Teff) {
+    for (int t_out = tl; t_out < g.T; t_out += (int)blockDim.y) {
       for (int v = 0; v < k::V; ++v) {
         for (int s = 0; s < k::NS; ++s) {
           double acc = op.invader[t_out * g.T + 0] * dudt(v, s, 0);
@@ -339,7 +344,7 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
       write_traces<D, P>(op, g, U_ader, g.T, t_out, c, tr, t_out);
     }
   } else {
-    for (int kk = tl; kk < k::V * k::NS; kk += Teff) {
+    for (int kk = tl; kk < k::V * k::NS; kk += (int)blockDim.y) {
       const int v = kk / k::NS, s = kk % k::NS;
       double acc = op.w_tp[0] * dudt(v, s, 0);
       for (int t = 1; t < g.T; ++t) acc = acc + op.w_tp[t] * dudt(v, s, t);

@@ -125,7 +125,11 @@ struct Stepper : StepperBase {
       const int mode = (it < m) ? 0 : final_mode;
       const double* Uin = (it == 0) ? C->U_sp : C->U_ader;
       const int Tu = (it == 0) ? 1 : C->T;
-      dim3 block(cpb, Teff);
+      // the first Picard iteration computes one time node but writes all T:
+      // T thread rows share its output (whole warps per row when cpb is a
+      // multiple of 32)
+      const int rows = (mode == 0 && Teff == 1 && cpb % 32 == 0) ? C->T : Teff;
+      dim3 block(cpb, rows);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
       {
         ProfScope ps_(C, "k_interior");
