@@ -94,6 +94,11 @@ __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, i
 // src/trouble_detection.py:10-13)
 template <int D>
 struct FvCandidate {
+// write_ext: 0 = no primitives (no limiting); 1 = W_old = prim(U_cv) and
+// W_new = prim(U_new) into ext_old / ext_new; 2 = as 1 with W_old read from
+// ext_new, which holds prim(U_cv) at this point (the previous substep's
+// W_new, refreshed by k_fv_correct where the fallback changed U_cv): the
+// same values without a second primitive conversion.
 static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, const double* __restrict__ dt_ptr,
                                            double w_i, const double* F0, const double* F1, const double* F2,
                                            const double* __restrict__ U_cv, double* __restrict__ U_new,
@@ -118,7 +123,12 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
   if (write_ext) {
     const long long e = ext_of<D>(g, ix, iy, iz);
     double W[V];
-    prim<D>(u, W, g.gamma, 0);
+    if (write_ext == 2) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) W[v] = ext_new[(long long)v * g.Nqe + e];
+    } else {
+      prim<D>(u, W, g.gamma, 0);
+    }
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_old[(long long)v * g.Nqe + e] = W[v];
     prim<D>(un, W, g.gamma, 0);
@@ -745,7 +755,8 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
                                            const unsigned long long* __restrict__ count, const double* F0,
                                            const double* F1, const double* F2, const double* B0, const double* B1,
                                            const double* B2, const double* A0, const double* A1, const double* A2,
-                                           const double* __restrict__ U_cv, double* __restrict__ U_new) {
+                                           const double* __restrict__ U_cv, double* __restrict__ U_new,
+                                           double* __restrict__ ext_new) {
   constexpr int V = D + 2;
   const unsigned long long cnt = *count;
   const double* FH[3] = {F0, F1, F2};
@@ -758,6 +769,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
   int ix, iy, iz;
   q_coords(g, q, ix, iy, iz);
   const int ii[3] = {ix, iy, iz};
+  double un[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     double acc = 0.0;
@@ -778,7 +790,17 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
       const double part = div_rcp(Fv[1] - Fv[0], fg.dx[d][ii[d]], fg.rdx[d][ii[d]]);
       acc = (d == 0) ? part : acc + part;
     }
-    U_new[(long long)v * g.Nq + q] = U_cv[(long long)v * g.Nq + q] - acc * dti;
+    un[v] = U_cv[(long long)v * g.Nq + q] - acc * dti;
+    U_new[(long long)v * g.Nq + q] = un[v];
+  }
+  if (ext_new != nullptr) {
+    // the primitives of the corrected state, which the next substep takes
+    // as its W_old (k_fv_candidate with w_old_from_ext)
+    double W[V];
+    prim<D>(un, W, g.gamma, 0);
+    const long long e = ext_of<D>(g, ix, iy, iz);
+#pragma unroll
+    for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
   }
   }
 }
@@ -788,9 +810,10 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
                              const long long* __restrict__ list, const unsigned long long* __restrict__ count,
                              const double* F0, const double* F1, const double* F2, const double* B0,
                              const double* B1, const double* B2, const double* A0, const double* A1,
-                             const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new) {
+                             const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new,
+                             double* __restrict__ ext_new) {
   FvCorrect<D>::run(hw_blk(), g, fg, dt_ptr, w_i, godunov, list, count, F0, F1, F2, B0, B1, B2, A0, A1, A2, U_cv,
-                    U_new);
+                    U_new, ext_new);
 }
 
 // dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when

@@ -222,7 +222,8 @@ struct Stepper : StepperBase {
       {
         ProfScope ps_(C, "k_fv_candidate");
         launch<FvCandidate<D>>(C, "k_fv_candidate", k_fv_candidate<D>, blocks_for(g.Nq, BS), BS, 0, g, C->fvg, C->dt,
-                               w_i, FH[0], FH[1], FH[2], C->U_cv, C->U_new, C->ext_old, C->ext_new, cf.FB ? 1 : 0);
+                               w_i, FH[0], FH[1], FH[2], C->U_cv, C->U_new, C->ext_old, C->ext_new,
+                               cf.FB ? (i == 0 ? 1 : 2) : 0);
       }
       CKL();
       if (cf.FB && C->tape_mode == 2) {
@@ -358,7 +359,7 @@ struct Stepper : StepperBase {
           }
           CKL();
         }
-        k_fv_correct_grid(C, w_i, FH);
+        k_fv_correct_grid(C, w_i, FH, i + 1 < C->T ? C->ext_new : nullptr);
         CKL();
         C->fb_ran = true;
         if (C->recording) {
@@ -403,14 +404,16 @@ struct Stepper : StepperBase {
                                                                C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt);
   }
 
-  void k_fv_correct_grid(spd_ctx* C, double w_i, const double* const* FH) {
+  // ext_new non-null: also the primitives of the corrected subcells, the
+  // next substep's W_old
+  void k_fv_correct_grid(spd_ctx* C, double w_i, const double* const* FH, double* ext_new) {
     const Geo& g = C->geo;
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nq, 128));
     {
       ProfScope ps_(C, "k_fv_correct");
       launch<FvCorrect<D>>(C, "k_fv_correct", k_fv_correct<D>, (unsigned)nb, 128, 0, g, C->fvg, C->dt, w_i,
                            C->cfg.godunov, C->list_q, C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
-                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new);
+                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new, ext_new);
     }
   }
 
