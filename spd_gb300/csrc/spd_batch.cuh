@@ -69,7 +69,7 @@ __device__ __forceinline__ void pack_call(const Blk& B, const Pack<H, R...>& p, 
 
 // instance of block b: the last i < n with boff[i] <= b (instances with no
 // blocks have boff[i] == boff[i+1] and are skipped)
-__device__ __forceinline__ int instance_of(const unsigned* __restrict__ boff, int n, unsigned b) {
+__host__ __device__ __forceinline__ int instance_of(const unsigned* __restrict__ boff, int n, unsigned b) {
   int lo = 0, hi = n;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
