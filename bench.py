@@ -396,7 +396,7 @@ def ours(args):
     U_host[...] = s.dm.U_sp
     W_host[...] = s.dm.W_cv
     out = torch.empty(int(np.prod(shape_u)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape_u)
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(args.steps, 10))
 
     def e2e_step():
         s._ctx.upload("U_sp", U_host)
