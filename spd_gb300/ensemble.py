@@ -74,7 +74,9 @@ class SDADER_Ensemble:
                                               ctypes.byref(h))
         if rc != 0:
             msg = self.lib.spd_ensemble_last_error(None)
-            raise _lib.SpdError(f"ensemble create failed with status {rc}: {msg.decode() if msg else ''}")
+            hint = ("; the packed form needs one dimension, degree, option set and cells per block "
+                    "(packed=False advances instances that differ)") if self.packed else ""
+            raise _lib.SpdError(f"ensemble create failed with status {rc}: {msg.decode() if msg else ''}{hint}")
         self._ens = h
 
     def graph_nodes(self) -> int:
