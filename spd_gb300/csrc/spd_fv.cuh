@@ -65,6 +65,10 @@ __device__ __forceinline__ double np_max_key(double a, double b) {
   if (is_nan_bits(b)) return b;
   return order_key(a) >= order_key(b) ? a : b;
 }
+// x != 0.0 on the bits (true for NaN, false for both zeros)
+__device__ __forceinline__ bool nonzero_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) != 0;
+}
 // x > 0 on the bits (false for zeros, negatives and NaN)
 __device__ __forceinline__ bool gt0_key(double x) {
   const long long b = __double_as_longlong(x);
@@ -143,6 +147,29 @@ __global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_pt
                                const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
                                double* ext_new, int write_ext) {
   FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext);
+}
+
+// W_cv (subcell layout) from the active region of an extended primitive
+// array: the end-of-step primitives when ext_new holds prim of the final
+// subcell state (src/sdader_simulator.py:351-359 computed once, in the last
+// substep's candidate update and corrected update)
+template <int D>
+struct ExtToPlain {
+  static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __restrict__ ext,
+                                             double* __restrict__ W_cv) {
+    constexpr int V = D + 2;
+    const long long q = B.id * (long long)blockDim.x + threadIdx.x;
+    if (q >= g.Nq) return;
+    int ix, iy, iz;
+    q_coords(g, q, ix, iy, iz);
+    const long long e = ext_of<D>(g, ix, iy, iz);
+#pragma unroll
+    for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = ext[(long long)v * g.Nqe + e];
+  }
+};
+template <int D>
+__global__ void k_ext_to_plain(Geo g, const double* __restrict__ ext, double* __restrict__ W_cv) {
+  ExtToPlain<D>::run(hw_blk(), g, ext, W_cv);
 }
 
 // ghost fill of one direction (src/fv_simulator.py:224-273): store the
@@ -553,7 +580,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int godun
     } else {
       a = aff[fidx];
     }
-    need = godunov || (a != 0.0);
+    need = godunov || nonzero_bits(a);
     if (need) {
       mark_cell[i1] = 1;
       mark_cell[i2] = 1;
@@ -794,8 +821,9 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
     U_new[(long long)v * g.Nq + q] = un[v];
   }
   if (ext_new != nullptr) {
-    // the primitives of the corrected state, which the next substep takes
-    // as its W_old (k_fv_candidate with w_old_from_ext)
+    // the primitives of the corrected state: the next substep's W_old
+    // (k_fv_candidate with write_ext == 2) or, after the last substep, W_cv
+    // (k_ext_to_plain)
     double W[V];
     prim<D>(un, W, g.gamma, 0);
     const long long e = ext_of<D>(g, ix, iy, iz);

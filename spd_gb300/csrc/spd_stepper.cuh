@@ -359,7 +359,7 @@ struct Stepper : StepperBase {
           }
           CKL();
         }
-        k_fv_correct_grid(C, w_i, FH, i + 1 < C->T ? C->ext_new : nullptr);
+        k_fv_correct_grid(C, w_i, FH, C->ext_new);
         CKL();
         C->fb_ran = true;
         if (C->recording) {
@@ -404,8 +404,8 @@ struct Stepper : StepperBase {
                                                                C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt);
   }
 
-  // ext_new non-null: also the primitives of the corrected subcells, the
-  // next substep's W_old
+  // ext_new non-null: also the primitives of the corrected subcells (the
+  // next substep's W_old, or the step's W_cv after the last substep)
   void k_fv_correct_grid(spd_ctx* C, double w_i, const double* const* FH, double* ext_new) {
     const Geo& g = C->geo;
     const long long nb = std::min<long long>(PERSIST_BLOCKS, blocks_for(g.Nq, 128));
@@ -440,6 +440,18 @@ struct Stepper : StepperBase {
     if (int r = predictor(C, final_mode)) return r;
     if (C->cfg.update == SPD_UPDATE_FV) {
       if (int r = fv_update(C)) return r;
+      if (C->cfg.FB) {
+        // W_cv = prim(U_cv) (src/sdader_simulator.py:376): ext_new already
+        // holds it (the last substep's W_new, refreshed where corrected)
+        const Geo& g = C->geo;
+        {
+          ProfScope ps_(C, "k_ext_to_plain");
+          launch<ExtToPlain<D>>(C, "k_ext_to_plain", k_ext_to_plain<D>, blocks_for(g.Nq, BS), BS, 0, g, C->ext_new,
+                                C->W_cv);
+        }
+        CKL();
+        return 0;
+      }
     }
     // W_cv = prim(U_cv) (src/sdader_simulator.py:376)
     return wcv(C);
