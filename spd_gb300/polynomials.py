@@ -98,15 +98,59 @@ def quadrature_points(mesh: np.ndarray, d: int, light: bool = True):
 
 
 def quadrature_mean(mesh: np.ndarray, fct: Callable, d: int, v: int, light: bool = True,
-                    points=None) -> np.ndarray:
+                    points=None, workers: int = 1) -> np.ndarray:
     """Cell means of fct(x, v) over the control volumes of ``mesh`` with a
     tensor Gauss-Legendre rule (src/polynomials.py:124-148).  ``points`` is
-    the result of quadrature_points(mesh, d, light) when already built."""
+    the result of quadrature_points(mesh, d, light) when already built.
+    fct is called once on all points, as in the reference; with workers > 1
+    the weighted sums run on thread slabs of cells (the same sum per cell)."""
     pts, w = points if points is not None else quadrature_points(mesh, d, light)
-    args = [fct(pts, v), (Ellipsis,) + tuple(range(d))]
-    for i in range(d):
-        args.extend([w, (i,)])
-    return np.einsum(*args)
+    vals = fct(pts, v)
+
+    def mean(block):
+        args = [block, (Ellipsis,) + tuple(range(d))]
+        for i in range(d):
+            args.extend([w, (i,)])
+        return np.einsum(*args)
+
+    return _on_slabs(mean, vals, workers)
+
+
+def _on_slabs(fn, arr: np.ndarray, workers: int) -> np.ndarray:
+    """fn(arr) computed as fn of slabs of the leading axis on host threads
+    (NumPy releases the GIL in its loops); fn must act on each index of that
+    axis on its own, so that the result is the same array, bit for bit."""
+    n0 = arr.shape[0]
+    if workers < 2 or n0 < 2:
+        return fn(arr)
+    bounds = np.linspace(0, n0, min(workers * 4, n0) + 1).astype(int)
+    first = fn(arr[bounds[0]:bounds[1]])
+    out = np.empty((n0,) + first.shape[1:], dtype=first.dtype)
+    out[bounds[0]:bounds[1]] = first
+
+    def one(k):
+        out[bounds[k]:bounds[k + 1]] = fn(arr[bounds[k]:bounds[k + 1]])
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(one, range(1, len(bounds) - 1)))
+    return out
+
+
+def quadrature_points_threaded(mesh: np.ndarray, d: int, light: bool = True, workers: int | None = None,
+                               min_cells: int = 1 << 15):
+    """quadrature_points on host thread slabs of the outermost cell axis
+    (each point is formed from its own cell's edges only: the same bits)."""
+    ncells = int(np.prod(mesh.shape[1:1 + d]))
+    workers = workers or min(16, os.cpu_count() or 1)
+    if ncells < min_cells or workers < 2:
+        return quadrature_points(mesh, d, light)
+    w = quadrature_points(mesh[:, :1], d, light)[1]
+    moved = np.moveaxis(mesh, 1, 0)
+    pts = _on_slabs(lambda m: np.moveaxis(quadrature_points(np.moveaxis(m, 0, 1), d, light)[0], 1, 0), moved,
+                    workers)
+    pts = np.ascontiguousarray(np.moveaxis(pts, 0, 1))
+    pts.setflags(write=False)
+    return pts, w
 
 
 def transform_axis(B: np.ndarray, A: np.ndarray, idim: int, ndim: int, ader: bool = False) -> np.ndarray:

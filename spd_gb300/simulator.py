@@ -12,6 +12,7 @@ step.
 from __future__ import annotations
 
 import ctypes
+import os
 from collections import defaultdict
 from timeit import default_timer as timer
 from typing import Callable, Tuple
@@ -23,7 +24,7 @@ import numpy as np
 from . import _lib
 from .initial_conditions import sine_wave
 from .polynomials import (ader_matrix, flux_points, gauss_legendre_quadrature, intfromsol_matrix,
-                          lagrange_matrix, lagrangeprime_matrix, quadrature_mean, quadrature_points,
+                          lagrange_matrix, lagrangeprime_matrix, quadrature_mean, quadrature_points_threaded,
                           solution_points, transform_axis, transform_full, transform_full_threaded)
 
 DIMS = ("x", "y", "z")
@@ -88,10 +89,13 @@ def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1):
     vels = np.arange(ndim) + 1
     mesh = mesh_cv(ndim, N, p, lims, Nghe, ops["x_fp"])
     W_gh = np.ndarray((nvar,) + tuple(N[i] + 2 * Nghe for i in range(ndim))[::-1] + (p + 1,) * ndim)
-    # the quadrature points are the same for every variable: built once
-    points = quadrature_points(mesh, ndim)
+    # the quadrature points are the same for every variable: built once;
+    # large grids build them and sum each variable on host thread slabs
+    ncells = int(np.prod([N[i] + 2 * Nghe for i in range(ndim)]))
+    workers = min(16, os.cpu_count() or 1) if ncells >= (1 << 15) else 1
+    points = quadrature_points_threaded(mesh, ndim, workers=workers)
     for var in range(nvar):
-        W_gh[var] = quadrature_mean(mesh, init_fct, ndim, var, points=points)
+        W_gh[var] = quadrature_mean(mesh, init_fct, ndim, var, points=points, workers=workers)
     del points
     W_init_cv = W_gh[(slice(None),) + (slice(Nghe, -Nghe),) * ndim + (Ellipsis,)]
     W_cv = W_init_cv.copy()

@@ -108,3 +108,21 @@ def test_initial_state_builds_quadrature_points_once():
     for var in range(4):
         assert np.array_equal(W_gh[var], quadrature_mean(mesh, fct, 2, var))
     assert np.array_equal(W_sp, transform_full(W_init_cv.copy(), ops["cv_to_sp"], 2))
+
+
+@pytest.mark.parametrize("ndim,p,N", [(1, 3, 4000), (2, 3, 150), (2, 2, 97), (3, 2, 24), (3, 3, 13)])
+def test_threaded_quadrature_is_bitwise(ndim, p, N):
+    """Quadrature points and per-variable cell means on thread slabs give
+    the same bits as the single-threaded forms."""
+    from spd_gb300.initial_conditions import four_quadrant, kelvin_helmholtz, sedov, sod
+    from spd_gb300.polynomials import quadrature_mean, quadrature_points, quadrature_points_threaded
+    from spd_gb300.simulator import mesh_cv
+    fct = {1: sod, 2: kelvin_helmholtz(N, seed=2) if p == 3 else four_quadrant, 3: sedov(N)}[ndim]
+    ops = SDADER_Simulator.build_operators(p, p)
+    mesh = mesh_cv(ndim, [N] * ndim, p, [(0.0, 1.0)] * ndim, 1, ops["x_fp"])
+    a, wa = quadrature_points(mesh, ndim)
+    b, wb = quadrature_points_threaded(mesh, ndim, workers=4, min_cells=1)
+    assert np.array_equal(a, b) and np.array_equal(wa, wb) and not b.flags.writeable
+    for v in range(ndim + 2):
+        assert np.array_equal(quadrature_mean(mesh, fct, ndim, v, points=(a, wa)),
+                              quadrature_mean(mesh, fct, ndim, v, points=(b, wb), workers=4))
