@@ -112,26 +112,47 @@ template <int N> SPD_FN bool operator<(const Dual<N>& a, double b) { return a.v 
 template <int N> SPD_FN bool operator>(const Dual<N>& a, double b) { return a.v > b; }
 
 // Correctly rounded a / b from a correctly rounded reciprocal rb = RN(1/b)
-// (b finite and nonzero) by Markstein's correction (P. Markstein, IBM J.
-// Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point
-// Arithmetic, 2nd ed., Thm. 5.3): q = RN(a*rb) is within one ulp of a/b, the
-// residual a - b*q is exact in one fused multiply-add, and RN(q + r*rb) is
-// RN(a/b) when nothing underflows.  When q is zero, infinite or NaN (zero,
-// infinite or NaN numerator; zero or infinite divisor) q itself has the IEEE
-// quotient's value and sign and is returned.  Three FP64 operations instead
-// of a full division where one divisor serves several quotients.
+// by Markstein's correction (P. Markstein, IBM J. Res. Dev. 34(1), 1990;
+// Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed., Thm. 5.3):
+// q = RN(a*rb) is within one ulp of a/b, the residual a - b*q is exact in
+// one fused multiply-add, and RN(q + r*rb) is RN(a/b).  The theorem needs
+// every quantity away from underflow and overflow, so the corrected quotient
+// is used only when the biased exponents of b lie in [23, 2023] and those of
+// a and q in [63, 2023] (then rb and q are normal, and the exact residual, a
+// multiple of ulp(b)*ulp(q) >= 2^-1074, is representable).  Outside that
+// window: a zero, infinite or NaN numerator or divisor makes q itself the
+// IEEE quotient (value and sign) and q is returned; any other operand pair
+// (subnormal or huge b, a or q near underflow or overflow) is divided by
+// IEEE division.  Three FP64 operations instead of a full division where
+// one divisor serves several quotients.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ double div_ieee_slow(double a, double b) { return a / b; }
+#else
+inline double div_ieee_slow(double a, double b) { return a / b; }
+#endif
+SPD_FN long long abs_bits_of(double x) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x) & 0x7fffffffffffffffLL;
+#else
+  long long bits;
+  memcpy(&bits, &x, sizeof(bits));
+  return bits & 0x7fffffffffffffffLL;
+#endif
+}
 SPD_FN double div_rcp(double a, double b, double rb) {
   const double q = a * rb;
   const double r = fma(-q, b, a);
   const double q2 = fma(r, rb, q);
-#ifdef __CUDA_ARCH__
-  const long long bits = __double_as_longlong(q) & 0x7fffffffffffffffLL;
-#else
-  long long bits;
-  memcpy(&bits, &q, sizeof(bits));
-  bits &= 0x7fffffffffffffffLL;
-#endif
-  return (bits == 0 || bits >= 0x7ff0000000000000LL) ? q : q2;
+  constexpr long long INF = 0x7ff0000000000000LL;
+  const long long ea = abs_bits_of(a) >> 52, eb = abs_bits_of(b) >> 52, eq = abs_bits_of(q) >> 52;
+  const long long ab = abs_bits_of(a), bb = abs_bits_of(b);
+  if (eb >= 23 && eb <= 2023) {
+    if (ab == 0 || ab >= INF) return q;
+    if (ea >= 63 && ea <= 2023 && eq >= 63 && eq <= 2023) return q2;
+  } else if (bb == 0 || bb >= INF) {
+    return q;
+  }
+  return div_ieee_slow(a, b);
 }
 
 SPD_FN double sval(double x) { return x; }

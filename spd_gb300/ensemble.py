@@ -133,8 +133,13 @@ class SDADER_Ensemble:
         """Time real ensemble steps for every candidate -- the packed form
         and the stream form with each number of streams, at each cells per
         block -- and keep the fastest.  The probe steps advance the
-        instances and count as steps."""
-        results = {}
+        instances and count as steps.  A candidate whose ensemble cannot be
+        created (the packed form for instances that differ in dimension,
+        degree or options) is skipped and listed in ``tuning["skipped"]``;
+        if no candidate builds, the form in use before the call is rebuilt
+        and the error is raised."""
+        prev = (self.packed, self.nstreams, self.cells_per_block())
+        results, skipped = {}, {}
         forms = [("packed", 0)] if True in packed else []
         if False in packed:
             forms += [("streams", ns) for ns in streams]
@@ -143,7 +148,11 @@ class SDADER_Ensemble:
             for form, ns in forms:
                 self.packed = form == "packed"
                 self.nstreams = ns or self.nstreams
-                self._build()
+                try:
+                    self._build()
+                except _lib.SpdError as err:
+                    skipped[(form, ns, cpb)] = str(err)
+                    continue
                 self._push_times()
                 self._check(self.lib.spd_ensemble_step(self._ens, 1), "warm-up")
                 self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
@@ -152,20 +161,28 @@ class SDADER_Ensemble:
                 self._check(self.lib.spd_ensemble_synchronize(self._ens), "synchronize")
                 results[(form, ns, cpb)] = (time.perf_counter() - t0) / probe_launches
                 self._sync_times((1 + probe_launches) * self.steps_per_launch)
+
+        def label(k):
+            return f"packed x{k[2]}" if k[0] == "packed" else f"{k[1]} streams x{k[2]}"
+
+        if not results:
+            self.packed, self.nstreams = prev[0], prev[1]
+            for s, (c, _) in zip(self.sims, prev[2]):
+                self.lib.spd_set_cells_per_block(s._ctx.h, c)
+            self._build()
+            raise _lib.SpdError("autotune: no candidate ensemble could be created: "
+                                + "; ".join(f"{label(k)}: {v}" for k, v in skipped.items()))
         best = min(results, key=results.get)
         form, ns, cpb = best
         self.packed = form == "packed"
         self.nstreams = ns or self.nstreams
         self.set_cells_per_block(cpb)
         self._build()
-
-        def label(k):
-            return f"packed x{k[2]}" if k[0] == "packed" else f"{k[1]} streams x{k[2]}"
-
         self.tuning = {"form": form, "streams": ns if form == "streams" else None, "cells_per_block": cpb,
                        "seconds_per_step": results[best] / self.steps_per_launch,
                        "graph_nodes_per_step": self.graph_nodes() // self.steps_per_launch,
-                       "candidates": {label(k): v for k, v in sorted(results.items(), key=lambda kv: kv[1])}}
+                       "candidates": {label(k): v for k, v in sorted(results.items(), key=lambda kv: kv[1])},
+                       "skipped": {label(k): v for k, v in skipped.items()}}
         return self.tuning
 
     def close(self):

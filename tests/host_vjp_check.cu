@@ -87,17 +87,34 @@ double check_flux_prim(std::mt19937_64& rng, int d) {
 
 // div_rcp (Markstein's correction from a correctly rounded reciprocal)
 // against the correctly rounded IEEE quotient: returns the mismatch count.
+// The operands cover the step's range, zeros, infinities and NaN, and the
+// edges of the exponent range: subnormal and huge divisors, numerators and
+// quotients near underflow and overflow, and subnormal quotients.
 long long check_div_rcp(std::mt19937_64& rng, long long n) {
-  std::uniform_int_distribution<int> ea(-80, 80), eb(-40, 40);
+  std::uniform_int_distribution<int> ea(-80, 80), eb(-40, 40), wide(-1074, 1023), edge(0, 120);
   std::uniform_real_distribution<double> m(1.0, 2.0);
   long long bad = 0;
   const double specials[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, 1.0, -1.0, 0.4, 3.0};
+  const double tiny[] = {4.9406564584124654e-324, 2.2250738585072009e-308, 2.2250738585072014e-308,
+                         1.0e-310, 1.7976931348623157e308, 8.98846567431158e307};
   for (long long i = 0; i < n; ++i) {
     double a = std::ldexp(m(rng), ea(rng)) * ((rng() & 1) ? -1.0 : 1.0);
     double b = std::ldexp(m(rng), eb(rng)) * ((rng() & 1) ? -1.0 : 1.0);
     if (i % 97 == 0) a = specials[(i / 97) % 9];
     if (i % 89 == 0) b = specials[5 + (i / 89) % 4];
     if (i % 7 == 0) b = 0.4;  // gamma - 1
+    if (i % 5 == 1) {
+      // anywhere in the exponent range, incl. subnormal operands
+      a = std::ldexp(m(rng), wide(rng)) * ((rng() & 1) ? -1.0 : 1.0);
+      b = std::ldexp(m(rng), wide(rng)) * ((rng() & 1) ? -1.0 : 1.0);
+    } else if (i % 5 == 3) {
+      // quotients and operands at the window's edges: near 2^-1022 and 2^1023
+      const int k = edge(rng);
+      a = std::ldexp(m(rng), (i & 8) ? -1080 + k : 1023 - k) * ((rng() & 1) ? -1.0 : 1.0);
+      b = std::ldexp(m(rng), (i & 16) ? 60 - k : k - 60);
+      if (i % 55 == 3) b = tiny[(i / 55) % 6];
+      if (i % 65 == 3) a = tiny[(i / 65) % 6];
+    }
     volatile double rb = 1.0 / b;
     const double got = div_rcp(a, b, rb);
     const double want = a / b;

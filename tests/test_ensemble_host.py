@@ -16,8 +16,9 @@ class FakeLib:
     adds 0.25 to each instance's device time; probe launches of the
     candidate (packed, cells per block 32) are the fastest."""
 
-    def __init__(self, fail_create=False):
+    def __init__(self, fail_create=False, fail_packed=False):
         self.fail_create = fail_create
+        self.fail_packed = fail_packed
         self.created = []
         self.times = {}
         self.cpb = {}
@@ -35,7 +36,7 @@ class FakeLib:
         return self._create("streams", nstreams, n, spl, ref)
 
     def _create(self, form, nstreams, n, spl, ref):
-        if self.fail_create:
+        if self.fail_create or (self.fail_packed and form == "packed"):
             self.last_err = b"instances differ at launch 3 (k_nad): options, degree or cells per block"
             return 1
         handle = len(self.created) + 1
@@ -125,6 +126,34 @@ def test_autotune_tries_every_candidate_and_keeps_the_fastest(fake):
     assert len(tuning["candidates"]) == 6
     assert fake.created[-1][0] == "packed"  # rebuilt with the choice
     assert all(s.n_step == 3 + 6 * 2 for s in sims)  # each probe: 1 warm-up + 1 timed step
+
+
+def test_autotune_skips_a_packed_form_that_cannot_be_created(monkeypatch):
+    """Instances that differ in degree or options: the packed create fails,
+    autotune keeps timing the stream forms and builds the fastest of them."""
+    lib = FakeLib(fail_packed=True)
+    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
+    sims = _sims(2)
+    e = ens_mod.SDADER_Ensemble(sims, packed=False, nstreams=2)
+    tuning = e.autotune(streams=(1, 4), cpbs=(16, 32), probe_launches=1)
+    assert tuning["form"] == "streams"
+    assert len(tuning["candidates"]) == 4 and len(tuning["skipped"]) == 2
+    assert all("instances differ" in v for v in tuning["skipped"].values())
+    assert e._ens is not None and lib.created[-1][0] == "streams"
+    e.perform_iterations(1)  # the chosen form is live
+
+
+def test_autotune_with_no_buildable_candidate_restores_the_previous_form(monkeypatch):
+    lib = FakeLib(fail_packed=True)
+    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
+    sims = _sims(2)
+    e = ens_mod.SDADER_Ensemble(sims, packed=False, nstreams=3)
+    with pytest.raises(_lib.SpdError, match="no candidate"):
+        e.autotune(streams=(1,), cpbs=(16,), probe_launches=1, packed=(True,))
+    assert lib.created[-1][:2] == ("streams", 3) and e._ens is not None
+    e.perform_iterations(1)
 
 
 def test_failed_create_explains_itself(monkeypatch):

@@ -47,6 +47,44 @@ def test_cfl_dt_noalloc_matches_compute_dt_twice():
     s.close()
 
 
+def test_cfl_dt_noalloc_partial_last_block_and_nan():
+    """30x30 cells at p=2: 8,100 subcells, so the last 256-thread block is
+    partly empty (its idle threads contribute 0).  Then a NaN planted in one
+    subcell on the host must come back as a NaN dt, as from compute_dt."""
+    import math
+    import torch
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300.initial_conditions import four_quadrant
+    s = SDADER_Simulator(p=2, N=(30, 30), init_fct=four_quadrant, update="FV", FB=True, riemann_solver_sd="hllc",
+                         riemann_solver_fv="hllc", BC=(("gradfree", "gradfree"),) * 2, verbose=False)
+    fn = _entry()
+    h = s.h_min / (s.p + 1)
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for call in range(2):
+        if call == 1:
+            s.perform_update()
+        s.compute_dt()
+        expected = s.dm.dt
+        W = torch.from_numpy(np.ascontiguousarray(s.transpose_to_fv(s.dm.W_cv))).cuda()
+        assert W[0].numel() % 256 != 0
+        rc = fn(W.data_ptr(), W[0].numel(), s.ndim, s.gamma, s.min_c2, s.cfl_coeff, h, out.data_ptr(), stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert out.item() == expected, (call, out.item(), expected)
+    W_sd = s.dm.W_cv
+    W_sd[0, 17, 3, 1, 2] = np.nan  # one subcell's density (SD layout)
+    s.dm.W_cv = W_sd
+    s.compute_dt()
+    assert math.isnan(s.dm.dt)
+    W = torch.from_numpy(np.ascontiguousarray(s.transpose_to_fv(W_sd))).cuda()
+    rc = fn(W.data_ptr(), W[0].numel(), s.ndim, s.gamma, s.min_c2, s.cfl_coeff, h, out.data_ptr(), stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert math.isnan(out.item())
+    s.close()
+
+
 def test_cfl_dt_noalloc_rejects_oversized_input():
     import torch
     fn = _entry()
