@@ -118,6 +118,18 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
     return fail(C, SPD_ERR_ARG, "bad Riemann solver");
   if (cfg->slope_limiter < 0 || cfg->slope_limiter > 1) return fail(C, SPD_ERR_ARG, "bad slope limiter");
   if (cfg->update != SPD_UPDATE_SD && cfg->update != SPD_UPDATE_FV) return fail(C, SPD_ERR_ARG, "bad update");
+  if (cfg->update == SPD_UPDATE_FV && cfg->FB) {
+    // src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros (the
+    // perturbation of the well-balanced mode, which is not implemented), so
+    // the reference's fallback flux at those faces is 0*NaN and its first
+    // step turns the boundary cells into NaN, its second step every cell
+    for (int d = 0; d < D; ++d)
+      for (int s = 0; s < 2; ++s)
+        if (cfg->BC[d][s] == SPD_BC_EQ)
+          return fail(C, SPD_ERR_ARG,
+                      "boundary 'eq' with the FV update and FB: the reference's fallback fluxes there are NaN "
+                      "(zero-density ghost subcells), which this build does not reproduce");
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(C, SPD_ERR_CUDA, "no CUDA device available (spd_gb300 has no CPU path)");

@@ -216,6 +216,16 @@ class SDADER_Simulator:
             raise AttributeError(slope_limiter)
         if update not in _lib.UPDATE:
             raise ValueError(f"update must be 'SD' or 'FV', got {update!r}")
+        if update == "FV" and FB and any(side == "eq" for b in BC[:len(N)] for side in b):
+            # src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros
+            # (the perturbation of the well-balanced mode, not implemented
+            # here); the reference's MUSCL-Hancock fluxes at those faces are
+            # then NaN, and theta*F_FB + (1-theta)*F_HO turns the boundary
+            # cells into NaN in the first step and every cell in the second
+            raise NotImplementedError(
+                "BC 'eq' with update='FV' and FB=True: the reference's fallback fluxes at those boundaries are "
+                "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
+                "first two steps; this combination is refused instead of reproducing a NaN state")
         self._ctx = None
         # ---- Simulator (src/simulator.py:10-126) ----------------------
         self.init_fct = init_fct

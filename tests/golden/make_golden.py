@@ -2,7 +2,7 @@
 
 Run once in a container where the reference's sources are present:
 
-    python tests/golden/make_golden.py /path/to/reference
+    python tests/golden/make_golden.py /path/to/reference [--only name,name] [--long]
 
 It imports the reference's NumPy implementation (``src/`` of jpalafou/spd,
 CuPy absent so the FP64 NumPy path runs), builds each case below, records
@@ -10,6 +10,13 @@ the constant operators and the initial state, advances the listed number of
 steps with ``compute_dt`` + ``perform_update`` (the body of
 ``perform_iterations``) and records the state after every case.  The
 fixtures are .npz files; ``case.json`` inside each describes the run.
+
+``--long`` makes the long-horizon fixtures in ``long/`` instead: 100 steps
+(or a run to t_end with the clip and stop of ``perform_time_evolution``),
+with the dt of every step and, with limiting, a CRC-32 and a count of the
+trouble mask after every step; the t_end vortex case also stores the L1
+density error against the exact (translated) vortex, computed with the
+reference's own quadrature.
 """
 from __future__ import annotations
 
@@ -57,6 +64,40 @@ CASES = {
 }
 
 
+# long-horizon cases: name -> (constructor kwargs, initial condition spec,
+# {"steps": n} or {"t_end": t})
+LONG_CASES = {
+    "vortex32_p3_fvfb_llf_100steps": (CASES["vortex32_p3_fvfb_llf"][0], ("vortex", {}), {"steps": 100}),
+    "vortex32_p3_fvfb_llf_t1": (CASES["vortex32_p3_fvfb_llf"][0], ("vortex", {}), {"t_end": 1.0}),
+    "quadrant32_p3_fvfb_hllc_gradfree_100steps": (dict(p=3, N=(32, 32), update="FV", FB=True,
+                                                       riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                                       BC=(("gradfree", "gradfree"),) * 2),
+                                                  ("four_quadrant", {}), {"steps": 100}),
+    # at 8^3 the reference's state takes negative densities from step ~20
+    # and becomes NaN at step 63: 60 steps pin the near-vacuum path
+    "sedov8_p2_fvfb_hllc_reflective_60steps": (dict(p=2, N=(8, 8, 8), update="FV", FB=True,
+                                                    riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                                    BC=(("reflective", "reflective"),) * 3),
+                                               ("sedov", {"N": 8}), {"steps": 60}),
+    # the final state of this one is stored as CRC-32 digests of its bytes
+    # (with its sum and largest magnitude), which keeps the fixture small
+    "sedov16_p2_fvfb_hllc_reflective_100steps": (dict(p=2, N=(16, 16, 16), update="FV", FB=True,
+                                                      riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                                      BC=(("reflective", "reflective"),) * 3),
+                                                 ("sedov", {"N": 16}), {"steps": 100, "digest_state": True}),
+    "kh32_p3_fvfb_hllc_moncen_100steps": (dict(p=3, N=(32, 32), update="FV", FB=True, riemann_solver_sd="hllc",
+                                               riemann_solver_fv="hllc", slope_limiter="moncen",
+                                               BC=(("periodic", "periodic"),) * 2),
+                                          ("kelvin_helmholtz", {"N": 32}), {"steps": 100}),
+    "sod64_p2_fvfb_llf_gradfree_t02": (dict(p=2, N=(64,), update="FV", FB=True, riemann_solver_sd="llf",
+                                            riemann_solver_fv="llf", BC=(("gradfree", "gradfree"),)),
+                                       ("sod", {}), {"t_end": 0.2}),
+    "step16_p3_sd_hllc_periodic_100steps": (dict(p=3, N=(16, 16), update="SD", riemann_solver_sd="hllc",
+                                                 BC=(("periodic", "periodic"),) * 2),
+                                            ("step_function", {}), {"steps": 100}),
+}
+
+
 def make_ic(spec):
     name, kw = spec
     if name == "vortex":
@@ -66,11 +107,13 @@ def make_ic(spec):
     return getattr(ics, name)
 
 
-def main(ref_root):
+def main(ref_root, only=None, long=False):
     sys.path.insert(0, os.path.join(ref_root, "src"))
     warnings.simplefilter("ignore")
     from sdader_simulator import SDADER_Simulator  # the reference
     import polynomials as rpoly
+    if long:
+        return main_long(SDADER_Simulator, rpoly, only)
 
     # setup operators for p = 1..4 (host-side pin)
     ops = {}
@@ -89,6 +132,8 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "operators.npz"), **ops)
 
     for name, (kw, icspec, steps) in CASES.items():
+        if only and name not in only:
+            continue
         init = make_ic(icspec)
         s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **kw)
         out = {
@@ -126,5 +171,100 @@ def main(ref_root):
               os.path.getsize(os.path.join(HERE, f"{name}.npz")) // 1024, "KB", flush=True)
 
 
+def _trouble_digest(s):
+    import zlib
+    t = np.ascontiguousarray(s.dm.troubles)
+    return zlib.crc32(t.tobytes()), float(t.sum())
+
+
+def main_long(SDADER_Simulator, rpoly, only):
+    out_dir = os.path.join(HERE, "long")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, (kw, icspec, run) in LONG_CASES.items():
+        if only and name not in only:
+            continue
+        init = make_ic(icspec)
+        s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **kw)
+        out = {
+            "sp_to_fp": s.dm.sp_to_fp, "fp_to_sp": s.dm.fp_to_sp, "dfp_to_sp": s.dm.dfp_to_sp,
+            "sp_to_cv": s.dm.sp_to_cv, "fp_to_cv": s.dm.fp_to_cv, "cv_to_sp": s.dm.cv_to_sp,
+            "x_tp": s.dm.x_tp, "w_tp": s.dm.w_tp, "invader": s.dm.invader, "x_sp": s.x_sp, "x_fp": s.x_fp,
+            "init_U_sp": s.dm.U_sp.copy(), "init_W_cv": s.dm.W_cv.copy(),
+        }
+        for d in s.dims:
+            out[f"init_BC_fp_{d}"] = getattr(s.dm, f"BC_fp_{d}").copy()
+            if s.update == "FV":
+                out[f"init_BC_fv_{d}"] = getattr(s.dm, f"BC_fv_{d}").copy()
+        limited = s.update == "FV" and s.FB
+        s.init_sim()
+        dts, crcs, counts = [], [], []
+        if "steps" in run:
+            # perform_iterations (src/sdader_simulator.py:394-399)
+            for _ in range(run["steps"]):
+                s.compute_dt()
+                dts.append(float(s.dm.dt))
+                s.perform_update()
+                if limited:
+                    c, n = _trouble_digest(s)
+                    crcs.append(c)
+                    counts.append(n)
+        else:
+            # perform_time_evolution (src/sdader_simulator.py:401-413)
+            t_end = run["t_end"]
+            while s.time < t_end:
+                s.compute_dt()
+                if s.time + s.dm.dt >= t_end:
+                    s.dm.dt = t_end - s.time
+                if s.dm.dt < 1E-14:
+                    break
+                dts.append(float(s.dm.dt))
+                s.perform_update()
+                if limited:
+                    c, n = _trouble_digest(s)
+                    crcs.append(c)
+                    counts.append(n)
+        if limited:
+            out["troubles"] = s.dm.troubles.copy()
+            out["theta"] = s.dm.theta.copy()
+            for d in s.dims:
+                out[f"affected_faces_{d}"] = getattr(s.dm, f"affected_faces_{d}").copy()
+            out["troubles_crc32"] = np.array(crcs, dtype=np.uint32)
+            out["troubles_count"] = np.array(counts)
+        s.end_sim()
+        out["dts"] = np.array(dts)
+        out["time"] = np.array(s.time)
+        out["n_step"] = np.array(s.n_step)
+        for key in ("U_sp", "W_cv"):
+            a = np.ascontiguousarray(getattr(s.dm, key))
+            if run.get("digest_state"):
+                import zlib
+                out[f"{key}_crc32"] = np.array(zlib.crc32(a.tobytes()), dtype=np.uint32)
+                out[f"{key}_sum"] = np.array(np.sum(a))
+                out[f"{key}_absmax"] = np.array(np.max(np.abs(a)))
+            else:
+                out[key] = a.copy()
+        meta = dict(kwargs={k: (list(map(list, v)) if k == "BC" else (list(v) if isinstance(v, tuple) else v))
+                            for k, v in kw.items()},
+                    ic=list(icspec), run=run, steps=len(dts))
+        if icspec[0] == "vortex" and "t_end" in run:
+            # exact solution: the vortex translated by (1, 1) * t_end
+            shift = 1.0 * run["t_end"]
+            exact_fct = ics.isentropic_vortex(center=(5.0 + shift, 5.0 + shift))
+            exact = s.crop(rpoly.quadrature_mean(s.mesh_cv, exact_fct, s.ndim, 0)[None])[0]
+            out["l1_density_error_vs_exact"] = np.array(np.mean(np.abs(s.dm.W_cv[0] - exact)))
+            meta["l1_density_error_vs_exact"] = float(out["l1_density_error_vs_exact"])
+        out["case_json"] = np.array(json.dumps(meta))
+        path = os.path.join(out_dir, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(name, "steps", len(dts), "time", s.time, "troubles", counts[-1] if counts else "-",
+              os.path.getsize(path) // 1024, "KB", flush=True)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("reference", help="root of the reference's sources (the directory holding src/)")
+    ap.add_argument("--only", default="", help="comma-separated case names")
+    ap.add_argument("--long", action="store_true", help="make the long-horizon fixtures in long/")
+    a = ap.parse_args()
+    main(a.reference, only=set(filter(None, a.only.split(","))), long=a.long)

@@ -12,13 +12,27 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 DIMS = ("x", "y", "z")
 
 
+LONG = os.path.join(GOLDEN, "long")
+
+
+def long_case_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(LONG, "*.npz")))
+
+
 def case_names():
     return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                   if not p.endswith("operators.npz"))
 
 
-def load(name):
-    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+def load_long(name):
+    """A long-horizon fixture: as ``load``; ``meta["run"]`` is {"steps": n}
+    or {"t_end": t}, and the arrays hold the dt of every step and, with
+    limiting, a CRC-32 and count of the trouble mask after every step."""
+    return load(name, LONG)
+
+
+def load(name, where=GOLDEN):
+    z = np.load(os.path.join(where, f"{name}.npz"))
     data = {k: z[k] for k in z.files}
     meta = json.loads(str(data.pop("case_json")))
     kw = dict(meta["kwargs"])
@@ -47,7 +61,12 @@ def oracle_from_golden(data, kw):
     p = kw["p"]
     lims = [kw.get(f"{d}lim", (0, 1)) for d in DIMS[:ndim]]
     ops = {k: data[k] for k in ("sp_to_fp", "dfp_to_sp", "sp_to_cv", "cv_to_sp", "w_tp", "invader", "x_fp")}
-    state = {"U_sp": data["init_U_sp"], "U_cv": data["init_U_cv"], "W_cv": data["init_W_cv"]}
+    from oracle.sdader_oracle import compute_conservatives
+    # long-horizon fixtures carry no initial U_cv: the step never reads it
+    # before recomputing it from U_sp (FV) or at the end of a run (SD)
+    U_cv = data["init_U_cv"] if "init_U_cv" in data else compute_conservatives(data["init_W_cv"], ndim,
+                                                                                 kw.get("gamma", 1.4))
+    state = {"U_sp": data["init_U_sp"], "U_cv": U_cv, "W_cv": data["init_W_cv"]}
     for d in DIMS[:ndim]:
         state[f"BC_fp_{d}"] = data[f"init_BC_fp_{d}"]
         if f"init_BC_fv_{d}" in data:
@@ -66,3 +85,58 @@ def oracle_from_golden(data, kw):
 def golden_operators(data):
     return {k: data[k] for k in ("sp_to_fp", "fp_to_sp", "dfp_to_sp", "sp_to_cv", "fp_to_cv", "cv_to_sp",
                                  "x_tp", "w_tp", "invader", "x_sp", "x_fp")}
+
+
+def trouble_digest(troubles):
+    """CRC-32 of the trouble mask's bytes and its count (the per-step pin of
+    the long-horizon fixtures)."""
+    import zlib
+    t = np.ascontiguousarray(np.asarray(troubles, dtype=np.float64))
+    return zlib.crc32(t.tobytes()), float(t.sum())
+
+
+def run_like_reference(sim, meta, limited, get_dt, set_dt, get_time, troubles):
+    """Advance ``sim`` (product or oracle) exactly as the reference's
+    perform_iterations / perform_time_evolution loops do (without their
+    end_sim); returns the dts and the per-step trouble digests."""
+    run = meta["run"]
+    dts, crcs, counts = [], [], []
+
+    def after():
+        if limited:
+            c, n = trouble_digest(troubles())
+            crcs.append(c)
+            counts.append(n)
+
+    if "steps" in run:
+        for _ in range(run["steps"]):
+            sim.compute_dt()
+            dts.append(get_dt())
+            sim.perform_update()
+            after()
+    else:
+        t_end = run["t_end"]
+        while get_time() < t_end:
+            sim.compute_dt()
+            if get_time() + get_dt() >= t_end:
+                set_dt(t_end - get_time())
+            if get_dt() < 1E-14:
+                break
+            dts.append(get_dt())
+            sim.perform_update()
+            after()
+    return dts, crcs, counts
+
+
+def state_matches(got, data, key):
+    """Bitwise comparison of a final state array with a fixture that holds
+    either the array or the CRC-32 digest of its bytes; returns (ok, info)."""
+    got = np.ascontiguousarray(np.asarray(got, dtype=np.float64))
+    if key in data:
+        ok = np.array_equal(got, data[key], equal_nan=True)
+        return ok, (None if ok else float(np.nanmax(np.abs(got - data[key]))))
+    import zlib
+    crc = zlib.crc32(got.tobytes())
+    ok = crc == int(data[f"{key}_crc32"])
+    return ok, (None if ok else (float(np.sum(got)), float(data[f"{key}_sum"]),
+                                 float(np.max(np.abs(got))), float(data[f"{key}_absmax"])))

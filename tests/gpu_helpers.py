@@ -12,7 +12,9 @@ def product_from_golden(data, kw, meta):
     from spd_gb300 import SDADER_Simulator
     s = SDADER_Simulator(init_fct=make_ic(meta["ic"]), operators=golden_operators(data), verbose=False, **kw)
     s.dm.U_sp = data["init_U_sp"]
-    s.dm.U_cv = data["init_U_cv"]
+    # long-horizon fixtures carry no initial U_cv: the step never reads it
+    # before recomputing it from U_sp (FV) or at the end of a run (SD)
+    s.dm.U_cv = data["init_U_cv"] if "init_U_cv" in data else s.compute_conservatives(data["init_W_cv"])
     s.dm.W_cv = data["init_W_cv"]
     return s
 

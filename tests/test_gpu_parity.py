@@ -173,10 +173,13 @@ OPTION_CASES = {
                            BC=(("gradfree", "gradfree"),) * 2),
     "p3_ic_pressure": dict(p=3, N=(8, 8), init="four_quadrant", update="FV", FB=True, riemann_solver_sd="hllc",
                            riemann_solver_fv="hllc", BC=(("ic", "ic"), ("pressure", "pressure"))),
-    # "eq" with the FV update (zero ghost states) blows up to NaN at once in
-    # the reference, through the fallback flux it evaluates on every face;
-    # the SD update exercises the "eq" element-boundary states
+    # "eq" with the FV update and limiting (zero ghost subcells) turns the
+    # reference's state into NaN in two steps and is refused at
+    # construction; the SD update and the FV update without limiting
+    # exercise the "eq" element-boundary states
     "p3_eq_1d_sd": dict(p=3, N=(16,), init="sod", update="SD", riemann_solver_sd="hllc", BC=(("eq", "eq"),)),
+    "p3_eq_2d_fv_nofb": dict(p=3, N=(8, 8), init="four_quadrant", update="FV", FB=False, riemann_solver_sd="hllc",
+                             BC=(("eq", "gradfree"), ("periodic", "eq"))),
     "p3_moncen_nosed_nopad": dict(p=3, N=(8, 8), init="four_quadrant", update="FV", FB=True,
                                   riemann_solver_sd="lhllc", riemann_solver_fv="llf", slope_limiter="moncen",
                                   SED=False, PAD=False, BC=(("reflective", "gradfree"), ("gradfree", "reflective"))),

@@ -81,6 +81,10 @@ def test_unsupported_options_raise():
         SDADER_Simulator(N=(4,), slope_limiter="superbee")
     with pytest.raises(TypeError):
         SDADER_Simulator(N=(4,), BC=(("open", "open"),))
+    # "eq" boundaries with the FV update and limiting: the reference's state
+    # becomes NaN in two steps (zero-density ghost subcells); refused
+    with pytest.raises(NotImplementedError, match="eq"):
+        SDADER_Simulator(N=(4, 4), update="FV", FB=True, BC=(("eq", "gradfree"), ("periodic", "periodic")))
 
 
 @pytest.mark.parametrize("ndim,p,N", [(1, 3, 3000), (2, 3, 40), (2, 2, 96), (3, 2, 20), (3, 4, 12)])
