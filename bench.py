@@ -147,19 +147,59 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def interior_bytes_per_step(D, p, T, cells):
-    """Compulsory HBM bytes of all k_interior launches of one step (the
-    predictor's fused flux / derivative / Picard kernel), FV update."""
-    n, nf, V = p + 1, p + 2, D + 2
+def interior_flops_per_cell_step(D, p, m, update):
+    """Algorithmic FP64 operations of the work of all k_interior launches of
+    one step, per cell (one operation per add, subtract, multiply, divide;
+    a square root would count one): the reference's own arithmetic for that
+    work, counted once -- the sp -> fp interpolation of the interior flux
+    points and the edge traces (src/transforms.py:3-25), U -> W and the Euler
+    flux at interior flux points (src/hydro.py:48-86,127-170), the flux
+    derivative and its division by h (src/sd_simulator.py:196-206), the
+    Picard update (src/sdader_simulator.py:194-200) and, with update="SD",
+    the final weighted update (:202-208).  The first Picard iteration's T
+    time nodes are equal and count once (the reference evaluates them T
+    times).  The per-point terms equal the instrumented oracle's counts
+    (oracle/flop_count.py, checked by tests/test_flop_count.py)."""
+    n, nf, V, T = p + 1, p + 2, D + 2, m + 1
     NS, NJ = n ** D, n ** (D - 1)
-    u_sp = V * NS * 8
-    u_ader = V * T * NS * 8
-    fi = 2 * D * V * T * NJ * 8
-    tr = 2 * D * V * T * NJ * 8
-    first = u_sp + 2 * D * V * NJ * 8 + u_ader + tr           # it = 0 (one time node)
-    mid = u_ader + u_sp + fi + u_ader + tr                      # 0 < it < m
-    last = u_ader + fi + D * V * T * NJ * nf * 8                # it = m, flux points out
-    return cells * (first + (T - 2) * mid + last), T
+    interp = 2 * n - 1                      # one flux-point value of one variable
+    prim = 3 * D + 3                        # U -> W at one point
+    flux = 4 * D + 6                        # Euler flux at one point
+    faces = D * NJ * (nf - 2) * (V * interp + prim + flux)    # interior flux points of one time node
+    dudt = V * NS * (D * 2 * nf + (D - 1))                       # sum_d dfp_to_sp(F)/h of one time node
+    picard = V * NS * T * (2 * T + 1)                            # invader contraction, *dt, U_sp -
+    traces = D * NJ * 2 * V * interp                             # edge traces of one time node
+    sd_update = V * NS * (2 * T + 1)                             # w_tp contraction, *dt, U_sp -
+    total = 0
+    for it in range(m + 1):
+        teff = 1 if it == 0 else T
+        total += faces * teff
+        if it < m:
+            total += dudt * teff + picard + traces * T
+        elif update == "SD":
+            total += dudt * teff + sd_update
+    return total
+
+
+def compulsory_bytes_per_cell_step(D, p):
+    """Compulsory HBM traffic of a step per cell: U_sp read and written once
+    (2 * V * (p+1)^D doubles)."""
+    return 2 * (D + 2) * (p + 1) ** D * 8
+
+
+# DRAM traffic (read + write bytes) and executed FP64 instructions (DADD +
+# DMUL + DFMA, thread level) of k_interior per cell and step, summed over
+# the (m+1) launches of a step; 2D, p = 3, FV update.  Source: one ncu
+# capture, --clock-control none -k regex:k_interior over the four launches of
+# one step, metrics dram__bytes_read.sum, dram__bytes_write.sum,
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, of
+# `python bench.py --cells N --steps 1 --warmup 1 --no-cpu-baseline`, divided
+# by the N^2 cells (both scale with the cell count; the full 512^2 workload
+# is not captured with more than one pass).  Keyed by (D, p, update, build).
+NCU_K_INTERIOR = {
+    (2, 3, "FV", "ieee"): {"cells_captured": 256 * 256, "dram_bytes": 4 * 448.170496e6 / 65536,
+                           "fp64_inst": 42966.0},
+}
 
 
 def fp64_peak_tflops():
@@ -353,12 +393,13 @@ def ours(args):
         s.compute_dt()
         s.perform_update()
     torch.cuda.synchronize()
-    ctx.profile_report()
     launches0 = ctx.launch_count()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ctx.profile(True)
+    # the timed region: compute_dt + perform_update per step, launch by
+    # launch, no per-kernel events (inputs are larger than L2: U_sp alone is
+    # 134 MB at 512^2, a step touches several GB)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         e0.record(stream)
@@ -367,14 +408,28 @@ def ours(args):
             s.perform_update()
         e1.record(stream)
         torch.cuda.synchronize()
-    ctx.profile(False)
     ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
     if dist:
         dist.barrier()
     launches = ctx.launch_count() - launches0
-    prof = ctx.profile_report()
     clocks = clk.summary()
     value = whole_job_rate(dof, args.steps, world, ms)
+
+    # a separate pass with a CUDA-event pair around every launch (on the
+    # library's stream) for the per-kernel split and the kernel roofline
+    prof_steps = max(1, min(args.steps, 5))
+    ctx.profile_report()
+    ctx.profile(True)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(prof_steps):
+        s.compute_dt()
+        s.perform_update()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ctx.profile(False)
+    prof = ctx.profile_report()
+    prof_ms = p0.elapsed_time(p1)
 
     # the same steps through perform_iterations' driver: one captured step
     # (CUDA graph) replayed per step, dt and time kept on the device
@@ -416,45 +471,54 @@ def ours(args):
            "h2d_bytes_per_step": int(U_host.nbytes + W_host.nbytes), "d2h_bytes_per_step": int(out.nbytes),
            "steps": e2e_steps}
 
-    # roofline of the dominant kernel
-    peak_gbs, peak_kind = measured_peaks()
-    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 1.0))
-    total_kernel_ms = sum(v[1] for v in prof.values())
-    D, p = len(kw["N"]), kw["p"]
-    roof = None
-    if top[0] == "k_interior":
-        bytes_step, nlaunch_per_step = interior_bytes_per_step(D, p, p + 1, cells)
-        per_launch_bytes = bytes_step / nlaunch_per_step
-        avg_s = top[1][1] / top[1][0] / 1e3
-        achieved = per_launch_bytes / avg_s / 1e9
-        # DRAM bytes (read + write) per k_interior launch from one ncu capture of
-        # the 2D p=3 four-quadrant step at 256^2 (mean over the 4 launches of a
-        # step: 329, 454, 454, 556 MB; profiles/k_interior_quadrant256_p3.md),
-        # scaled by the cell count (traffic grows in proportion)
-        traffic = 448.170496e6 * cells / 65536 if (D, p) == (2, 3) else None
-        roof = {"bound": "hbm", "kernel": "k_interior", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved / peak_gbs, "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3}
-    fp64 = None
+    # roofline of the dominant kernel: the FP64 pipe binds (the step moves
+    # ~1 KB of compulsory HBM traffic per cell and computes ~1e5 operations)
+    fp64, fp64_clocks = None, None
     if rank == 0:
         try:
-            fp64 = fp64_peak_tflops()
+            with ClockSampler(local) as clk64:
+                fp64 = fp64_peak_tflops()
+            fp64_clocks = clk64.summary()
         except Exception:
             fp64 = None
-    # The binding roof: the FP64 pipe.  k_interior executes 42,966 FP64
-    # instructions (DADD + DMUL + DFMA, thread level) per cell and step in
-    # 2D at p=3 with the FV update, whatever the data (ncu smsp__sass_thread_inst_executed_op_
-    # {dadd,dmul,dfma}_pred_on.sum over the 4 launches of a 256^2 step / 65,536
-    # cells; profiles/k_interior_quadrant256_p3.md).  The peak is the issue
-    # rate cuBLAS DGEMM reaches (one DFMA per 2 flops).
-    fp64_roof = None
-    if roof is not None and fp64 and (D, p) == (2, 3) and kw.get("update") == "FV":
-        k_ms_step = prof["k_interior"][1] / args.steps
-        rate = 42966.0 * cells / (k_ms_step / 1e3)
-        peak = fp64 * 1e12 / 2.0
-        fp64_roof = {"bound": "fp64 pipe", "kernel": "k_interior", "achieved": rate / 1e9, "peak": peak / 1e9,
-                     "unit": "G FP64 instructions/s", "frac": rate / peak,
-                     "peak_kind": "measured (cuBLAS DGEMM issue rate)"}
+    D, p = len(kw["N"]), kw["p"]
+    m = p
+    upd = kw.get("update", "SD")
+    roof, issue, hbm = None, None, None
+    kint = prof.get("k_interior")
+    if kint:
+        flops_step = interior_flops_per_cell_step(D, p, m, upd) * cells
+        nlaunch = kint[0] / prof_steps
+        per_launch_flops = flops_step / nlaunch
+        avg_s = kint[1] / kint[0] / 1e3
+        achieved = per_launch_flops / avg_s / 1e12
+        ncu = NCU_K_INTERIOR.get((D, p, upd, "ieee"))
+        roof = {"bound": "fp64", "kernel": "k_interior", "achieved": achieved,
+                "peak": fp64, "unit": "TFLOP/s", "frac": (achieved / fp64) if fp64 else None,
+                "peak_kind": "measured in this run: cuBLAS DGEMM 8192^3 FP64 (burst; no FP64 entry in "
+                             "MEASURED_PEAKS.json)",
+                "traffic": ncu["dram_bytes"] * cells / nlaunch if ncu else None,
+                "traffic_kind": (f"ncu DRAM read+write per launch at {int(ncu['cells_captured'] ** 0.5)}^2 cells, "
+                                 "scaled by the cell count") if ncu else None,
+                "algorithmic_flops_per_launch": per_launch_flops,
+                "algorithmic_flops_per_cell_step": interior_flops_per_cell_step(D, p, m, upd),
+                "launches_per_step": nlaunch, "avg_launch_ms": avg_s * 1e3}
+        if ncu and fp64:
+            rate = ncu["fp64_inst"] * cells * prof_steps / (kint[1] / 1e3)
+            peak_issue = fp64 * 1e12 / 2.0
+            issue = {"kernel": "k_interior", "fp64_instructions_per_cell_step": ncu["fp64_inst"],
+                     "achieved_g_inst_per_s": rate / 1e9, "peak_g_inst_per_s": peak_issue / 1e9,
+                     "frac": rate / peak_issue,
+                     "meaning": "FP64 pipe occupancy: executed DADD+DMUL+DFMA (each 1) against cuBLAS DGEMM's "
+                                "DFMA issue rate; not a flop fraction"}
+    peak_gbs, peak_kind = measured_peaks()
+    hb = compulsory_bytes_per_cell_step(D, p) * cells / (ms / args.steps / 1e3) / 1e9
+    hbm = {"compulsory_bytes_per_cell_step": compulsory_bytes_per_cell_step(D, p), "achieved": hb,
+           "peak": peak_gbs, "unit": "GB/s", "frac": hb / peak_gbs, "peak_kind": peak_kind}
+    total_kernel_ms = sum(v[1] for v in prof.values())
+    fma = None
+    if rank == 0 and world == 1 and not args.no_fma:
+        fma = fma_build_section(args, kw, s, stream, dof, cells, fp64, ms / args.steps)
     line = None
     if rank == 0:
         cpu = None
@@ -476,19 +540,94 @@ def ours(args):
                            "l2": "inputs larger than L2: U_sp alone is "
                                  f"{dof * (D + 2) * 8 / 1e6:.0f} MB, step working set several GB"},
                 "roofline": roof,
-                "roofline_fp64": fp64_roof,
-                "fp64_gemm_peak_tflops": fp64,
+                "fp64_issue": issue,
+                "fma_build": fma,
+                "hbm_compulsory": hbm,
+                "fp64_gemm_peak_tflops": fp64, "fp64_gemm_clocks": fp64_clocks,
                 "cpu_baseline": cpu, "parity_vs_oracle": parity,
-                "vortex_t1": vortex_t1_error() if args.workload == "vortex32" else None,
+                "vortex_t1": vortex_t1_error() if world == 1 else None,
                 "graph_driver": graph_driver,
                 "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks,
-                "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
-                "kernel_share_of_step": total_kernel_ms / ms if ms else None}
+                "profiled_pass": {"steps": prof_steps, "ms_per_step": prof_ms / prof_steps,
+                                  "kernels_ms": {k: round(v[1], 3)
+                                                 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+                                  "kernel_share_of_step": total_kernel_ms / prof_ms if prof_ms else None}}
         print(json.dumps(line), flush=True)
     s.close()
     if dist:
         dist.destroy_process_group()
+
+
+def fma_build_section(args, kw, s_ieee, stream, dof, cells, fp64, ieee_ms_step):
+    """The same workload on the library built with fused multiply-adds
+    (SDADER_Simulator(fma=True)): its step time (timed like the headline),
+    its k_interior flop-basis roofline, and its deviation from the product
+    build (bit-identical to the reference) over 10 steps from the same
+    initial state: normwise relative difference of U_sp per variable and the
+    steps whose trouble masks differ."""
+    import numpy as np
+    import torch
+    from spd_gb300 import SDADER_Simulator
+    try:
+        f = SDADER_Simulator(verbose=False, fma=True, **kw)
+    except ImportError as err:
+        return {"unavailable": str(err)}
+    ctx = f._ctx
+    ctx.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        f.compute_dt()
+        f.perform_update()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        f.compute_dt()
+        f.perform_update()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    prof_steps = max(1, min(args.steps, 5))
+    ctx.profile_report()
+    ctx.profile(True)
+    for _ in range(prof_steps):
+        f.compute_dt()
+        f.perform_update()
+    torch.cuda.synchronize()
+    ctx.profile(False)
+    prof = ctx.profile_report()
+    D, p = len(kw["N"]), kw["p"]
+    kint = prof.get("k_interior")
+    roof = None
+    if kint:
+        achieved = interior_flops_per_cell_step(D, p, p, kw.get("update", "SD")) * cells * prof_steps / (
+            kint[1] / 1e3) / 1e12
+        roof = {"kernel": "k_interior", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+                "frac": achieved / fp64 if fp64 else None, "avg_launch_ms": kint[1] / kint[0]}
+    f.close()
+    # deviation from the product build over 10 steps from one initial state
+    # (fresh simulators: the FV boundary buffers start from the initial
+    # condition in both)
+    a = SDADER_Simulator(verbose=False, **kw)
+    f = SDADER_Simulator(verbose=False, fma=True, **kw)
+    limited = a.update == "FV" and a.FB
+    flips, devs = 0, {}
+    for k in range(10):
+        a.compute_dt()
+        f.compute_dt()
+        a.perform_update()
+        f.perform_update()
+        if limited and not np.array_equal(a.dm.troubles, f.dm.troubles):
+            flips += 1
+        if k in (0, 9):
+            Ua, Uf = a.dm.U_sp, f.dm.U_sp
+            devs[f"after_{k + 1}_steps"] = max(float(np.max(np.abs(Uf[v] - Ua[v])) / np.max(np.abs(Ua[v])))
+                                               for v in range(Ua.shape[0]))
+    a.close()
+    f.close()
+    return {"value": dof / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "speedup_over_product_build": ieee_ms_step / ms,
+            "roofline": roof, "normwise_rel_dev_U_sp": devs, "steps_with_trouble_mask_differences": flips,
+            "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:8]}}
 
 
 def ensemble_arm(args):
@@ -757,6 +896,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fma", action="store_true", help="skip the fused multiply-add build's section")
     ap.add_argument("--instances", type=int, default=64, help="ensemble size (kh_ensemble)")
     ap.add_argument("--ensemble-form", default="auto", choices=["auto", "packed", "streams"],
                     help="batched form (kh_ensemble): autotuned, or fixed without tuning")

@@ -12,6 +12,9 @@ import os
 import numpy as np
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libspd_gb300.so")
+# the opt-in build with fused multiply-adds (results differ from the
+# reference's in the last bits; see spd_gb300.build)
+LIB_PATH_FMA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libspd_gb300_fma.so")
 
 SPD_OK, SPD_ERR_ARG, SPD_ERR_CUDA, SPD_ERR_NONFINITE = 0, 1, 2, 3
 RIEMANN = {"llf": 0, "hllc": 1, "lhllc": 2}
@@ -87,19 +90,20 @@ class SpdError(RuntimeError):
     """Error reported by the CUDA library."""
 
 
-_LIB = None
+_LIBS = {}
 
 
-def load():
-    """Load the library once and declare the signatures."""
-    global _LIB
-    if _LIB is not None:
-        return _LIB
-    if not os.path.exists(LIB_PATH):
+def load(variant: str = "ieee"):
+    """Load a library variant once ("ieee": the product, bit-identical to
+    the reference; "fma": fused multiply-adds) and declare the signatures."""
+    if variant in _LIBS:
+        return _LIBS[variant]
+    path = {"ieee": LIB_PATH, "fma": LIB_PATH_FMA}[variant]
+    if not os.path.exists(path):
         raise ImportError(
-            f"{LIB_PATH} is missing: build it with spd_gb300.build.build() "
+            f"{path} is missing: build it with spd_gb300.build.build() "
             "(spd_gb300 has no CPU fallback)")
-    lib = ctypes.CDLL(LIB_PATH)
+    lib = ctypes.CDLL(path)
     vp = ctypes.c_void_p
     lib.spd_create.argtypes = [ctypes.POINTER(spd_config), ctypes.POINTER(spd_operators), ctypes.POINTER(vp)]
     lib.spd_upload.argtypes = [vp, ctypes.c_int, _dp, ctypes.c_size_t]
@@ -129,7 +133,8 @@ def load():
         getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int
     lib.spd_last_error.restype = ctypes.c_char_p
     lib.spd_version.restype = ctypes.c_char_p
-    _LIB = lib
+    lib.spd_variant = variant
+    _LIBS[variant] = lib
     return lib
 
 
@@ -141,8 +146,9 @@ def as_ptr(a: np.ndarray):
 class Context:
     """Owns one spd_ctx (one CUDA stream, device state of one simulation)."""
 
-    def __init__(self, cfg: spd_config, mats: dict, faces: list):
-        self.lib = load()
+    def __init__(self, cfg: spd_config, mats: dict, faces: list, variant: str = "ieee"):
+        self.lib = load(variant)
+        self.variant = variant
         self._keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in mats.items()}
         self._faces = [np.ascontiguousarray(f, dtype=np.float64) for f in faces]
         ops = spd_operators()

@@ -31,7 +31,10 @@ class SDADER_Ensemble:
         self.sims = list(simulators)
         if not self.sims:
             raise ValueError("empty ensemble")
-        self.lib = _lib.load()
+        variants = {getattr(s._ctx, "variant", "ieee") for s in self.sims}
+        if len(variants) > 1:
+            raise ValueError("an ensemble needs every instance built from one library (all fma=True or none)")
+        self.lib = _lib.load(variants.pop())
         self._declare()
         self.nstreams = nstreams
         self.steps_per_launch = steps_per_launch

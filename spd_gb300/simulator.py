@@ -156,6 +156,12 @@ class SDADER_Simulator:
     chain SDADER_Simulator -> SD_Simulator -> FV_Simulator -> Simulator.
     Options the GPU path does not implement (viscosity, potential, WB,
     isothermal, predictor=False) raise NotImplementedError.
+
+    Two keywords have no counterpart in the reference: ``operators`` (the
+    constant operator matrices, when the caller has them already) and
+    ``fma``: True runs the step from the library built with fused
+    multiply-adds (one FP64 instruction and one rounding per a*b+c instead
+    of two), which is faster but no longer bit-identical to the reference.
     """
 
     def __init__(self,
@@ -198,7 +204,8 @@ class SDADER_Simulator:
                               ("periodic", "periodic"),
                               ("periodic", "periodic")),
                  verbose=True,
-                 operators: dict | None = None):
+                 operators: dict | None = None,
+                 fma: bool = False):
         for flag, name in ((isothermal, "isothermal"), (viscosity, "viscosity"),
                            (potential, "potential"), (WB, "WB")):
             if flag:
@@ -227,6 +234,7 @@ class SDADER_Simulator:
                 "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
                 "first two steps; this combination is refused instead of reproducing a NaN state")
         self._ctx = None
+        self.fma = bool(fma)
         # ---- Simulator (src/simulator.py:10-126) ----------------------
         self.init_fct = init_fct
         self.eq_fct = eq_fct
@@ -426,7 +434,7 @@ class SDADER_Simulator:
         cfg.min_P = self.min_P
         cfg.godunov = int(bool(self.godunov))
         faces = [self.faces[DIMS[i]] for i in range(self.ndim)]
-        self._ctx = _lib.Context(cfg, self.ops, faces)
+        self._ctx = _lib.Context(cfg, self.ops, faces, variant="fma" if self.fma else "ieee")
 
     def _init_boundaries(self, U_sp, W_gh):
         """Initial boundary arrays: element edge traces of the initial state

@@ -27,9 +27,10 @@ def test_library_exports_every_declared_symbol():
     from spd_gb300 import _lib
     from spd_gb300.build import build
     build()
-    lib = ctypes.CDLL(_lib.LIB_PATH)
-    missing = [n for n in declared() if not hasattr(lib, n)]
-    assert not missing, missing
+    for path in (_lib.LIB_PATH, _lib.LIB_PATH_FMA):
+        lib = ctypes.CDLL(path)
+        missing = [n for n in declared() if not hasattr(lib, n)]
+        assert not missing, (path, missing)
     assert set(_lib.EXPORTS) <= set(declared())
 
 

@@ -94,7 +94,7 @@ def _sims(n):
 @pytest.fixture
 def fake(monkeypatch):
     lib = FakeLib()
-    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(_lib, "load", lambda *a: lib)
     monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
     return lib
 
@@ -132,7 +132,7 @@ def test_autotune_skips_a_packed_form_that_cannot_be_created(monkeypatch):
     """Instances that differ in degree or options: the packed create fails,
     autotune keeps timing the stream forms and builds the fastest of them."""
     lib = FakeLib(fail_packed=True)
-    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(_lib, "load", lambda *a: lib)
     monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
     sims = _sims(2)
     e = ens_mod.SDADER_Ensemble(sims, packed=False, nstreams=2)
@@ -146,7 +146,7 @@ def test_autotune_skips_a_packed_form_that_cannot_be_created(monkeypatch):
 
 def test_autotune_with_no_buildable_candidate_restores_the_previous_form(monkeypatch):
     lib = FakeLib(fail_packed=True)
-    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(_lib, "load", lambda *a: lib)
     monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
     sims = _sims(2)
     e = ens_mod.SDADER_Ensemble(sims, packed=False, nstreams=3)
@@ -158,7 +158,7 @@ def test_autotune_with_no_buildable_candidate_restores_the_previous_form(monkeyp
 
 def test_failed_create_explains_itself(monkeypatch):
     lib = FakeLib(fail_create=True)
-    monkeypatch.setattr(_lib, "load", lambda: lib)
+    monkeypatch.setattr(_lib, "load", lambda *a: lib)
     monkeypatch.setattr(ens_mod.SDADER_Ensemble, "_declare", lambda self: None)
     with pytest.raises(_lib.SpdError, match="packed=False"):
         ens_mod.SDADER_Ensemble(_sims(2))
