@@ -384,7 +384,7 @@ def ours(args):
     from spd_gb300 import SDADER_Simulator
     kw = workload_kwargs(args.workload, args.cells)
     dof, cells = dof_of(kw)
-    s = SDADER_Simulator(verbose=False, **kw)
+    s = SDADER_Simulator(verbose=False, fma=args.build == "fma", **kw)
     ctx = s._ctx
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
@@ -431,6 +431,12 @@ def ours(args):
     prof = ctx.profile_report()
     prof_ms = p0.elapsed_time(p1)
 
+    if args.lean:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
+                          "build": args.build, "lean": True,
+                          "kernels_ms": {k: round(v[1], 3) for k, v in prof.items()}}), flush=True)
+        s.close()
+        return
     # the same steps through perform_iterations' driver: one captured step
     # (CUDA graph) replayed per step, dt and time kept on the device
     s.time, _, _ = ctx.step(1, 0.0, 0, s.time)  # capture (untimed)
@@ -492,7 +498,7 @@ def ours(args):
         per_launch_flops = flops_step / nlaunch
         avg_s = kint[1] / kint[0] / 1e3
         achieved = per_launch_flops / avg_s / 1e12
-        ncu = NCU_K_INTERIOR.get((D, p, upd, "ieee"))
+        ncu = NCU_K_INTERIOR.get((D, p, upd, args.build))
         roof = {"bound": "fp64", "kernel": "k_interior", "achieved": achieved,
                 "peak": fp64, "unit": "TFLOP/s", "frac": (achieved / fp64) if fp64 else None,
                 "peak_kind": "measured in this run: cuBLAS DGEMM 8192^3 FP64 (burst; no FP64 entry in "
@@ -517,7 +523,7 @@ def ours(args):
            "peak": peak_gbs, "unit": "GB/s", "frac": hb / peak_gbs, "peak_kind": peak_kind}
     total_kernel_ms = sum(v[1] for v in prof.values())
     fma = None
-    if rank == 0 and world == 1 and not args.no_fma:
+    if rank == 0 and world == 1 and not args.no_fma and args.build == "ieee":
         fma = fma_build_section(args, kw, s, stream, dof, cells, fp64, ms / args.steps)
     line = None
     if rank == 0:
@@ -531,7 +537,7 @@ def ours(args):
                    "sample": f"1 step of the same configuration at {'x'.join([str(sample_n)] * len(kw['N']))} cells on one core "
                              "(CPU restatement of the reference's NumPy path)"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "build": args.build,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOADS[args.workload] + (f" (reduced to {args.cells} cells per side)"
                                                                    if args.cells else ""),
@@ -897,6 +903,12 @@ def main():
     ap.add_argument("--workload", default="quadrant512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fma", action="store_true", help="skip the fused multiply-add build's section")
+    ap.add_argument("--lean", action="store_true",
+                    help="only the timed and profiled passes (no graph driver, end-to-end, DGEMM, vortex, CPU "
+                         "baseline or fma sections): a short launch sequence for profilers")
+    ap.add_argument("--build", default="ieee", choices=["ieee", "fma"],
+                    help="library of the headline simulator: the product (bit-identical to the reference) or the "
+                         "fused multiply-add build")
     ap.add_argument("--instances", type=int, default=64, help="ensemble size (kh_ensemble)")
     ap.add_argument("--ensemble-form", default="auto", choices=["auto", "packed", "streams"],
                     help="batched form (kh_ensemble): autotuned, or fixed without tuning")
