@@ -72,7 +72,15 @@ enum spd_field {
   SPD_BC_FV_X = 11,
   SPD_BC_FV_Y = 12,
   SPD_BC_FV_Z = 13,
-  SPD_U_SP_ADJ = 14  /* adjoint of U_sp (U_sp layout), input and output of spd_vjp_step */
+  SPD_U_SP_ADJ = 14, /* adjoint of U_sp (U_sp layout), input and output of spd_vjp_step */
+  /* read-only, update FV only: the flux-point fluxes of the last step's
+   * final Picard iteration after the transverse subcell averaging, i.e. the
+   * reference's F_ader_fp_<dim> after switch_to_finite_volume
+   * (src/sdader_simulator.py:297-298); raw device layout [t][v][face], faces
+   * x-fastest with N_d*(p+1)+1 faces along d and N*(p+1) along the others */
+  SPD_F_FACES_X = 15,
+  SPD_F_FACES_Y = 16,
+  SPD_F_FACES_Z = 17
 };
 
 /* Constructor options of SDADER_Simulator (src/simulator.py:10-36,

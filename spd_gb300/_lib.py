@@ -26,6 +26,7 @@ FIELD = {
     "affected_faces_x": 5, "affected_faces_y": 6, "affected_faces_z": 7,
     "BC_fp_x": 8, "BC_fp_y": 9, "BC_fp_z": 10,
     "BC_fv_x": 11, "BC_fv_y": 12, "BC_fv_z": 13, "U_sp_adj": 14,
+    "F_faces_x": 15, "F_faces_y": 16, "F_faces_z": 17,
 }
 
 # every entry point declared in include/spd_gb300.h

@@ -423,6 +423,12 @@ static size_t field_count(spd_ctx* C, int field) {
       const int d = field - SPD_BC_FV_X;
       return d < D ? (size_t)2 * V * NGH * n_other_ext(g, d) : 0;
     }
+    case SPD_F_FACES_X:
+    case SPD_F_FACES_Y:
+    case SPD_F_FACES_Z: {
+      const int d = field - SPD_F_FACES_X;
+      return (d < D && C->F_HO[d]) ? (size_t)C->T * V * n_faces_host(g, d) : 0;
+    }
     default: return 0;
   }
 }
@@ -513,6 +519,7 @@ int spd_download(spd_ctx* C, int field, double* host, size_t count) {
   if (field == SPD_TROUBLES) src = C->troubles;
   else if (field == SPD_THETA) src = C->theta_final;
   else if (field >= SPD_AFFECTED_X && field <= SPD_AFFECTED_Z) src = C->aff[field - SPD_AFFECTED_X];
+  else if (field >= SPD_F_FACES_X && field <= SPD_F_FACES_Z) src = C->F_HO[field - SPD_F_FACES_X];
   if (field >= SPD_BC_FV_X && field <= SPD_BC_FV_Z) {
     const int d = field - SPD_BC_FV_X;
     if (!C->bcbuf[d]) return fail(C, SPD_ERR_ARG, "download: no FV boundary buffers (update is SD)");

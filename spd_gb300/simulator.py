@@ -134,6 +134,8 @@ class _DataManager:
         if name in _DataManager._device_fields and sim._ctx is not None:
             return sim._download(name)
         host = object.__getattribute__(self, "_host")
+        if name.startswith("F_ader_fp_") and name not in host and sim._ctx is not None:
+            return sim._F_ader_fp(name[-1])
         if name in host:
             return host[name]
         raise AttributeError(name)
@@ -149,37 +151,12 @@ class _DataManager:
         object.__getattribute__(self, "_host")[name] = value
 
 
-class SDADER_Simulator:
-    """SD-ADER simulator for the compressible Euler equations (GPU step).
-
-    Positional and keyword arguments follow the reference's constructor
-    chain SDADER_Simulator -> SD_Simulator -> FV_Simulator -> Simulator.
-    Options the GPU path does not implement (viscosity, potential, WB,
-    isothermal, predictor=False) raise NotImplementedError.
-
-    Two keywords have no counterpart in the reference: ``operators`` (the
-    constant operator matrices, when the caller has them already) and
-    ``fma``: True runs the step from the library built with fused
-    multiply-adds (one FP64 instruction and one rounding per a*b+c instead
-    of two), which is faster but no longer bit-identical to the reference.
-    """
+class Simulator:
+    """Base of the simulator classes (src/simulator.py:9-209): geometry,
+    variable indices, options and the host-side layout helpers.  It holds no
+    device state, as the reference's base class holds no step."""
 
     def __init__(self,
-                 FB: bool = False,
-                 tolerance: float = 1e-5,
-                 SED: bool = True,
-                 NAD: str = "",
-                 PAD: bool = True,
-                 blending: bool = True,
-                 min_rho: float = 1e-10,
-                 max_rho: float = 1e10,
-                 min_P: float = 1e-10,
-                 godunov: bool = False,
-                 riemann_solver_sd: str = "llf",
-                 update: str = "SD",
-                 riemann_solver_fv: str = "llf",
-                 slope_limiter: str = "minmod",
-                 predictor: bool = True,
                  init_fct: Callable = sine_wave,
                  eq_fct: Callable = sine_wave,
                  p: int = 1,
@@ -203,39 +180,10 @@ class SDADER_Simulator:
                  BC: Tuple = (("periodic", "periodic"),
                               ("periodic", "periodic"),
                               ("periodic", "periodic")),
-                 verbose=True,
-                 operators: dict | None = None,
-                 fma: bool = False):
-        for flag, name in ((isothermal, "isothermal"), (viscosity, "viscosity"),
-                           (potential, "potential"), (WB, "WB")):
-            if flag:
-                raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
-        if not predictor:
-            raise NotImplementedError("predictor=False (plain MUSCL) is not implemented "
-                                      "(the reference's path raises AttributeError)")
-        if Nghc != 2:
-            raise NotImplementedError("only Nghc=2 subcell ghost layers are supported")
-        if riemann_solver_sd not in _lib.RIEMANN:
-            raise AttributeError(riemann_solver_sd)
-        if riemann_solver_fv not in _lib.RIEMANN:
-            raise AttributeError(riemann_solver_fv)
-        if slope_limiter not in _lib.LIMITER:
-            raise AttributeError(slope_limiter)
-        if update not in _lib.UPDATE:
-            raise ValueError(f"update must be 'SD' or 'FV', got {update!r}")
-        if update == "FV" and FB and any(side == "eq" for b in BC[:len(N)] for side in b):
-            # src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros
-            # (the perturbation of the well-balanced mode, not implemented
-            # here); the reference's MUSCL-Hancock fluxes at those faces are
-            # then NaN, and theta*F_FB + (1-theta)*F_HO turns the boundary
-            # cells into NaN in the first step and every cell in the second
-            raise NotImplementedError(
-                "BC 'eq' with update='FV' and FB=True: the reference's fallback fluxes at those boundaries are "
-                "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
-                "first two steps; this combination is refused instead of reproducing a NaN state")
-        self._ctx = None
-        self.fma = bool(fma)
-        # ---- Simulator (src/simulator.py:10-126) ----------------------
+                 verbose=True):
+        if not hasattr(self, "_ctx"):
+            self._ctx = None
+        # ---- src/simulator.py:37-126 ----------------------------------
         self.init_fct = init_fct
         self.eq_fct = eq_fct
         if m == -1:
@@ -301,12 +249,116 @@ class SDADER_Simulator:
         self._p_ = ndim + 1
         self.nvar = ndim + 2
         self.rank = 0
-        # ---- FV_Simulator / SD_Simulator options ----------------------
+
+    def shape(self, idim):
+        return (None,) * (self.ndim - idim) + (slice(None),) + (None,) * idim
+
+    def domain_size(self):
+        return [self.N[dim] * self.n[dim] for dim in self.dims]
+
+    def regular_faces(self):
+        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim] + 1) for dim in self.dims]
+
+    def regular_centers(self):
+        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim]) for dim in self.dims]
+
+    def crop(self, M, ngh=1) -> np.ndarray:
+        return M[(slice(None),) + (slice(ngh, -ngh),) * self.ndim + (Ellipsis,)]
+
+    def compute_primitives(self, U, **kwargs) -> np.ndarray:
+        return _primitives(U, self.vels, self._p_, self.gamma)
+
+    def compute_conservatives(self, W, **kwargs) -> np.ndarray:
+        return _conservatives(W, self.vels, self._p_, self.gamma)
+
+    def compute_positions(self):
+        pass
+
+    def compute_mesh_cv(self):
+        pass
+
+    def post_init(self):
+        pass
+
+    def compute_dt(self) -> None:
+        pass
+
+
+class FV_Simulator(Simulator):
+    """The finite-volume base class (src/fv_simulator.py:10-285): Riemann
+    solver, slope limiter and predictor options and the subcell array
+    shapes.  Like the reference's, it holds no step of its own; the
+    subcell update runs inside SDADER_Simulator's step on the GPU."""
+
+    def __init__(self, riemann_solver_fv: str = "llf", slope_limiter: str = "minmod", predictor: bool = True,
+                 *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        if riemann_solver_fv not in _lib.RIEMANN:
+            raise AttributeError(riemann_solver_fv)
+        if slope_limiter not in _lib.LIMITER:
+            raise AttributeError(slope_limiter)
         self.riemann_solver_fv_name = riemann_solver_fv
-        self.riemann_solver_sd_name = riemann_solver_sd
         self.slope_limiter_name = slope_limiter
         self.predictor = predictor
+
+    def array_FV(self, nvar, dim=None, ngh=0) -> np.ndarray:
+        """src/fv_simulator.py:24-29 (one value per cell)."""
+        N = [self.N[d2] + (dim == d2) + 2 * ngh for d2 in self.dims]
+        return np.ndarray([nvar] + N[::-1])
+
+    def array_FV_BC(self, dim="x") -> np.ndarray:
+        """src/fv_simulator.py:31-37."""
+        ngh = self.Nghc
+        N = [self.N[d2] + 2 * ngh if dim != d2 else ngh for d2 in self.dims]
+        return np.ndarray([2, self.nvar] + N[::-1])
+
+
+class SD_Simulator(Simulator):
+    """The spectral-difference class (src/sd_simulator.py:19-239): constant
+    operators, mesh, initial state and the CFL dt, with the state on the
+    GPU.  Constructed on its own it steps with the SD update and no
+    limiter; SDADER_Simulator (its subclass) adds the options of the
+    reference's SDADER class.  Options the GPU step does not implement
+    (viscosity, potential, WB, isothermal, predictor=False) raise
+    NotImplementedError here, before any device work.
+    """
+
+    def __init__(self, riemann_solver_sd: str = "llf", update: str = "SD", *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        for flag, name in ((self.isothermal, "isothermal"), (self.viscosity, "viscosity"),
+                           (self.potential, "potential"), (self.WB, "WB")):
+            if flag:
+                raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
+        # options of the classes below SD_Simulator in the reference's chain
+        # (FV_Simulator, SDADER_Simulator), at their defaults when absent
+        for key, val in (("riemann_solver_fv_name", "llf"), ("slope_limiter_name", "minmod"), ("predictor", True),
+                         ("FB", False), ("tolerance", 1e-5), ("SED", True), ("NAD", ""), ("PAD", True),
+                         ("blending", True), ("min_rho", 1e-10), ("max_rho", 1e10), ("min_P", 1e-10),
+                         ("godunov", False), ("fma", False), ("_operators", None)):
+            if not hasattr(self, key):
+                setattr(self, key, val)
+        if not self.predictor:
+            raise NotImplementedError("predictor=False (plain MUSCL) is not implemented "
+                                      "(the reference's path raises AttributeError)")
+        if self.Nghc != 2:
+            raise NotImplementedError("only Nghc=2 subcell ghost layers are supported")
+        if riemann_solver_sd not in _lib.RIEMANN:
+            raise AttributeError(riemann_solver_sd)
+        if update not in _lib.UPDATE:
+            raise ValueError(f"update must be 'SD' or 'FV', got {update!r}")
+        if update == "FV" and self.FB and any(side == "eq" for d in self.dims for side in self.BC[d]):
+            # src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros
+            # (the perturbation of the well-balanced mode, not implemented
+            # here); the reference's MUSCL-Hancock fluxes at those faces are
+            # then NaN, and theta*F_FB + (1-theta)*F_HO turns the boundary
+            # cells into NaN in the first step and every cell in the second
+            raise NotImplementedError(
+                "BC 'eq' with update='FV' and FB=True: the reference's fallback fluxes at those boundaries are "
+                "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
+                "first two steps; this combination is refused instead of reproducing a NaN state")
+        self.riemann_solver_sd_name = riemann_solver_sd
         self.update = update
+        p, m, ndim = self.p, self.m, self.ndim
         # ---- SD_Simulator operators (src/sd_simulator.py:30-52) ------------
         self.x, self.w = gauss_legendre_quadrature(0.0, 1.0, p)
         sp = solution_points(0.0, 1.0, p)
@@ -319,31 +371,19 @@ class SDADER_Simulator:
             self.fp[dim] = fp
             setattr(self, f"n{dim}", p + 1)
             self.n[dim] = p + 1
-        if operators is None:
-            operators = self.build_operators(p, m)
+        operators = self._operators if self._operators is not None else self.build_operators(p, m)
         self.ops = operators
         for key in ("sp_to_fp", "fp_to_sp", "dfp_to_sp", "sp_to_cv", "fp_to_cv", "cv_to_sp",
                     "x_tp", "w_tp", "invader"):
             if key in operators:
                 setattr(self.dm, key, operators[key])
         self.nader = m + 1
-        # ---- SDADER options -------------------------------------------
-        self.FB = FB
-        self.tolerance = tolerance
-        self.SED = SED
-        self.NAD = NAD
-        self.PAD = PAD
-        self.blending = blending
-        self.min_rho = min_rho
-        self.max_rho = max_rho
-        self.min_P = min_P
-        self.godunov = godunov
         # ---- geometry and initial state (src/sd_simulator.py:59-90) ----
         self.mesh_cv = self.compute_mesh_cv()
         self.compute_positions()
         W_gh, self.W_init_cv, W_sp, U_sp, U_cv = initial_state(
             ndim, [self.N[d] for d in self.dims], p, [self.lim[d] for d in self.dims], self.init_fct,
-            operators, gamma, Nghe)
+            operators, self.gamma, self.Nghe)
         W_cv = self.W_init_cv.copy()
         self.dm.W_sp = W_sp
         # ---- device context ----------------------------------------------
@@ -353,6 +393,7 @@ class SDADER_Simulator:
         self._ctx.upload("W_cv", W_cv)
         self._init_boundaries(U_sp, W_gh)
         self.compute_dt()
+
 
     # ------------------------------------------------------------------
     # setup
@@ -470,29 +511,8 @@ class SDADER_Simulator:
                 self._ctx.upload(f"BC_fv_{dim}", np.stack([M[tuple(lo)], M[tuple(hi)]]))
 
     # ------------------------------------------------------------------
-    # layouts and host-side helpers (src/simulator.py, src/sd_simulator.py)
+    # layouts and host-side helpers (src/sd_simulator.py)
     # ------------------------------------------------------------------
-    def shape(self, idim):
-        return (None,) * (self.ndim - idim) + (slice(None),) + (None,) * idim
-
-    def domain_size(self):
-        return [self.N[dim] * self.n[dim] for dim in self.dims]
-
-    def regular_faces(self):
-        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim] + 1) for dim in self.dims]
-
-    def regular_centers(self):
-        return [np.linspace(self.lim[dim][0], self.lim[dim][1], self.N[dim] * self.n[dim]) for dim in self.dims]
-
-    def crop(self, M, ngh=1) -> np.ndarray:
-        return M[(slice(None),) + (slice(ngh, -ngh),) * self.ndim + (Ellipsis,)]
-
-    def compute_primitives(self, U, **kwargs) -> np.ndarray:
-        return _primitives(U, self.vels, self._p_, self.gamma)
-
-    def compute_conservatives(self, W, **kwargs) -> np.ndarray:
-        return _conservatives(W, self.vels, self._p_, self.gamma)
-
     def array(self, px, py, pz, ngh=0, ader=False) -> np.ndarray:
         shape = [self.nvar, self.nader] if ader else [self.nvar]
         Ns = [self.N[dim] + 2 * ngh for dim in self.dims][::-1]
@@ -501,6 +521,81 @@ class SDADER_Simulator:
 
     def array_sp(self, **kwargs):
         return self.array(self.p + 1, self.p + 1, self.p + 1, **kwargs)
+
+    def array_fp(self, dims="xyz", **kwargs):
+        """Flux-point array shape (src/sd_simulator.py:150-156)."""
+        p = self.p
+        return self.array(p + 1 + ("x" in dims), p + 1 + ("y" in dims), p + 1 + ("z" in dims), **kwargs)
+
+    def array_RS(self, dim="x", ader=False) -> np.ndarray:
+        """Riemann-problem array shape (src/sd_simulator.py:158-166)."""
+        shape = [self.nvar, self.nader] if ader else [self.nvar]
+        shape += [self.N[d2] + (d2 == dim) for d2 in self.dims][::-1]
+        shape += [self.p + 1] * (self.ndim - 1)
+        return np.ndarray(shape)
+
+    def array_BC(self, dim="x", ader=False) -> np.ndarray:
+        """Domain-boundary array shape (src/sd_simulator.py:168-182)."""
+        shape = [2, self.nvar, self.nader] if ader else [2, self.nvar]
+        if self.Z and dim in ("x", "y"):
+            shape += [self.N["z"]]
+        if self.Y and dim in ("x", "z"):
+            shape += [self.N["y"]]
+        if dim in ("y", "z"):
+            shape += [self.N["x"]]
+        shape += [self.p + 1] * (self.ndim - 1)
+        return np.ndarray(shape)
+
+    def integrate_faces(self, M_fp, dim, ader=True):
+        """Subcell averages across the directions other than ``dim``
+        (src/sd_simulator.py:208-212)."""
+        for other in self.dims:
+            if other != dim:
+                M_fp = transform_axis(M_fp, self.ops["sp_to_cv"], self.dims[other], self.ndim, ader=ader)
+        return M_fp
+
+    def compute_sp_from_dfp_x(self, ader=True):
+        """src/sd_simulator.py:199-200 on ``dm.F_ader_fp_x``."""
+        return self.compute_sp_from_dfp(self.dm.F_ader_fp_x, "x", ader=ader) / self.dx
+
+    def compute_sp_from_dfp_y(self, ader=True):
+        return self.compute_sp_from_dfp(self.dm.F_ader_fp_y, "y", ader=ader) / self.dy
+
+    def compute_sp_from_dfp_z(self, ader=True):
+        return self.compute_sp_from_dfp(self.dm.F_ader_fp_z, "z", ader=ader) / self.dz
+
+    def _F_ader_fp(self, d):
+        """``dm.F_ader_fp_<d>`` after a step with the FV update: the last
+        Picard iteration's flux-point fluxes averaged across the other
+        directions (what the reference's array holds after
+        switch_to_finite_volume, src/sdader_simulator.py:297-298), in its
+        layout (V, T, [Nz,] [Ny,] Nx, [nz,] [ny,] nx) with p+2 points along
+        d.  The SD update keeps no flux-point array on the device."""
+        if d not in self.dims:
+            raise AttributeError(f"F_ader_fp_{d}")
+        if self.update != "FV":
+            raise AttributeError(f"F_ader_fp_{d} is kept on the device only with update='FV'")
+        idim = self.dims[d]
+        n, T, V, nd = self.p + 1, self.nader, self.nvar, self.ndim
+        X = [self.N[DIMS[i]] * n for i in range(nd)]
+        FX = [X[i] + (1 if i == idim else 0) for i in range(nd)]
+        raw = self._ctx.download(f"F_faces_{d}", (T, V, int(np.prod(FX))))
+        # face index of (cell c_i, point k_i): coordinate c_i*n + k_i along
+        # each direction i, faces x-fastest; reference axes are
+        # (cells z, y, x, points z, y, x) for the directions present
+        fid = np.zeros([1] * (2 * nd), dtype=np.int64)
+        stride = 1
+        for i in range(nd):
+            npts = n + 1 if i == idim else n
+            coord = np.arange(self.N[DIMS[i]])[:, None] * n + np.arange(npts)[None, :]
+            shp = [1] * (2 * nd)
+            shp[nd - 1 - i] = self.N[DIMS[i]]
+            shp[2 * nd - 1 - i] = npts
+            # place the (cell, point) grid on axes (nd-1-i, 2nd-1-i)
+            fid = fid + np.moveaxis(coord.reshape(coord.shape + (1,) * (2 * nd - 2)), [0, 1],
+                                    [nd - 1 - i, 2 * nd - 1 - i]).reshape(shp) * stride
+            stride *= FX[i]
+        return raw[:, :, fid].transpose((1, 0) + tuple(range(2, 2 + 2 * nd)))
 
     def transpose_to_fv(self, M):
         if self.ndim == 1:
@@ -666,6 +761,61 @@ class SDADER_Simulator:
             self._ctx = None
 
 
-class SD_Simulator(SDADER_Simulator):
-    """Name kept for callers that construct the SD base class directly; it
-    is the same object as SDADER_Simulator with its defaults."""
+class SDADER_Simulator(SD_Simulator, FV_Simulator):
+    """SD-ADER simulator for the compressible Euler equations (GPU step).
+
+    Positional and keyword arguments follow the reference's constructor
+    chain SDADER_Simulator -> SD_Simulator -> FV_Simulator -> Simulator
+    (src/sdader_simulator.py:14-59).
+
+    Two keywords have no counterpart in the reference: ``operators`` (the
+    constant operator matrices, when the caller has them already) and
+    ``fma``: True runs the step from the library built with fused
+    multiply-adds (one FP64 instruction and one rounding per a*b+c instead
+    of two), which is faster but no longer bit-identical to the reference.
+    """
+
+    def __init__(self,
+                 FB: bool = False,
+                 tolerance: float = 1e-5,
+                 SED: bool = True,
+                 NAD: str = "",
+                 PAD: bool = True,
+                 blending: bool = True,
+                 min_rho: float = 1e-10,
+                 max_rho: float = 1e10,
+                 min_P: float = 1e-10,
+                 godunov: bool = False,
+                 *args,
+                 operators: dict | None = None,
+                 fma: bool = False,
+                 **kwargs):
+        self._ctx = None
+        # the SDADER options are set before the chain below runs, because
+        # SD_Simulator creates the device context with all of them
+        self.FB = FB
+        self.tolerance = tolerance
+        self.SED = SED
+        self.NAD = NAD
+        self.PAD = PAD
+        self.blending = blending
+        self.min_rho = min_rho
+        self.max_rho = max_rho
+        self.min_P = min_P
+        self.godunov = godunov
+        self._operators = operators
+        self.fma = bool(fma)
+        super().__init__(*args, **kwargs)
+
+    def array_FV(self, n, nvar, dim=None, ngh=0) -> np.ndarray:
+        """src/sdader_simulator.py:273-278 (n subcells per cell and
+        direction)."""
+        N = [self.N[d2] * n + (dim == d2) + 2 * ngh for d2 in self.dims]
+        return np.ndarray([nvar] + N[::-1])
+
+    def array_FV_BC(self, dim="x") -> np.ndarray:
+        """src/sdader_simulator.py:280-286."""
+        ngh = self.Nghc
+        N = [self.N[d2] * self.n[d2] + 2 * ngh if dim != d2 else ngh for d2 in self.dims]
+        return np.ndarray([2, self.nvar] + N[::-1])
+

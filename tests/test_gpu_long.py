@@ -39,6 +39,7 @@ def test_gpu_long_horizon_step_by_step(name):
     def set_dt(v):
         s.dm.dt = v
 
+    s.init_sim()
     dts, crcs, counts = run_like_reference(s, meta, limited, lambda: s.dm.dt, set_dt, lambda: s.time,
                                            lambda: s.dm.troubles)
     s.n_step = len(dts)
