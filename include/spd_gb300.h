@@ -108,6 +108,12 @@ typedef struct spd_config {
   double min_rho, max_rho, min_P;
   int godunov;
   int BC[3][2];          /* spd_bc per direction and side */
+  /* viscosity (src/simulator.py:23-28, src/sdader_simulator.py:245-268):
+   * the SD update, or the FV update without FB (the reference's viscous
+   * fallback fluxes raise AttributeError, src/muscl.py:253) */
+  int viscosity;
+  double nu;
+  double beta;
 } spd_config;
 
 /* Constant operators built at setup on the host

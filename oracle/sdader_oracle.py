@@ -312,6 +312,25 @@ def compute_fluxes(W, vels, gamma):
     return xp.stack([comp[v] for v in range(ndim + 2)], 0)
 
 
+def viscous_fluxes(W, vels, dUs, nu, beta):
+    """src/hydro.py:172-241: viscous fluxes of the conservative variables
+    from the primitives W and their gradients dUs[direction], in the
+    rotated velocity order ``vels``; the density component is 0*rho*nu."""
+    ndim = len(vels)
+    _p_ = ndim + 1
+    v1 = vels[0]
+    dU1 = dUs[v1 - 1]
+    comp = {}
+    comp[v1] = 2 * dU1[v1] - beta * dU1[v1]
+    comp[_p_] = W[v1] * comp[v1]
+    for vel in vels[1:]:
+        dU = dUs[vel - 1]
+        comp[v1] = comp[v1] - beta * dU[vel]
+        comp[vel] = dU1[vel] + dU[v1]
+        comp[_p_] = comp[_p_] + W[vel] * comp[vel]
+    return xp.stack([(comp[v] if v else xp.zeros(W[0].shape, W)) * W[0] * nu for v in range(ndim + 2)], 0)
+
+
 def compute_cs(P, rho, gamma, min_c2):
     """src/hydro.py:3-46: sqrt of gamma*P/rho floored at min_c2 (NaN -> floor)."""
     c2 = gamma * P / rho
@@ -483,7 +502,7 @@ class OracleSDADER:
     def __init__(self, *, ndim, N, p, m, lims, BC, gamma, cfl_coeff, min_c2,
                  riemann_solver_sd, riemann_solver_fv, slope_limiter, update,
                  FB, tolerance, SED, NAD, PAD, blending, min_rho, max_rho,
-                 min_P, godunov, ops, state, Nghc=2):
+                 min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3):
         self.ndim = ndim
         self.N = list(N)          # cells per dim, x first
         self.p = p
@@ -510,6 +529,9 @@ class OracleSDADER:
         self.max_rho = max_rho
         self.min_P = min_P
         self.godunov = godunov
+        self.viscosity = viscosity
+        self.nu = nu
+        self.beta = beta
         self.ngh = Nghc
         self.ops = {k: (_Mat(v) if k in ("sp_to_fp", "dfp_to_sp", "sp_to_cv", "cv_to_sp", "invader", "w_tp")
                         else v) for k, v in ops.items()}
@@ -583,6 +605,9 @@ class OracleSDADER:
         c_max = float(c.max())
         h = self.h_min / (self.p + 1)
         dt = h / c_max if c_max == c_max else float("nan")
+        if self.viscosity and self.nu > 0:
+            # Python's min keeps its first argument unless the second is smaller
+            dt = min(dt, h ** 2 / self.nu * .25)
         self.dt = self.cfl * dt
         return self.dt
 
@@ -591,7 +616,7 @@ class OracleSDADER:
         """Returns F_ader_fp per dim with Riemann fluxes at element edges."""
         ops = self.ops
         nd = self.ndim
-        F_all = {}
+        F_all, M_all = {}, {}
         for idim in range(nd):
             vels = self.rolled_vels(idim)
             ax_sp = sp_axis(nd, idim)
@@ -600,41 +625,88 @@ class OracleSDADER:
             # interior flux points (the edge values are replaced below)
             M_in = _shift(M_fp, 1, -1, ax_sp)
             F_in = compute_fluxes(compute_primitives(M_in, nd, self.gamma), vels, self.gamma)
-            # edge traces (src/sd_boundary.py:7-17)
-            left_trace = xp.take(M_fp, 0, ax_sp)
-            right_trace = xp.take(M_fp, self.nf - 1, ax_sp)
-            tax = ax_cell + 1
-            Ncell = self.N[idim]
-            first_l = xp.take(left_trace, 0, tax)
-            last_r = xp.take(right_trace, Ncell - 1, tax)
-            bc = []
-            for side in (0, 1):
-                kind = self.BC[idim][side]
-                if kind == "periodic":
-                    v = last_r if side == 0 else first_l
-                elif kind in ("reflective", "gradfree"):
-                    v = first_l if side == 0 else last_r
-                    if kind == "reflective":
-                        v = xp.stack([v[k] * -1 if k == idim + 1 else v[k] for k in range(self.V)], 0)
-                elif kind in ("ic", "eq", "pressure"):
-                    b = self.BC_fp[idim][side]
-                    v = (b.expand(first_l.shape) if self.torch_mode
-                         else np.broadcast_to(b, first_l.shape).copy())
-                else:
-                    raise TypeError("Undetermined boundary type")
-                bc.append(v)
-            # pressure sides overwrite the edge traces with the stored state
-            if self.BC[idim][0] == "pressure":
-                left_trace = xp.cat([xp.expand(bc[0], tax), _shift(left_trace, 1, None, tax)], tax)
-            if self.BC[idim][1] == "pressure":
-                right_trace = xp.cat([_shift(right_trace, None, -1, tax), xp.expand(bc[1], tax)], tax)
-            ML = xp.cat([xp.expand(bc[0], tax), right_trace], tax)
-            MR = xp.cat([left_trace, xp.expand(bc[1], tax)], tax)
+            ML, MR = self._interfaces(M_fp, idim)
             F = riemann(self.rs_sd, ML, MR, vels, self.gamma, self.min_c2, prims=False)
-            # scatter (src/sd_boundary.py:19-30)
-            F_all[idim] = xp.cat([xp.expand(_shift(F, None, -1, tax), ax_sp), F_in,
-                                  xp.expand(_shift(F, 1, None, tax), ax_sp)], ax_sp)
+            F_all[idim] = xp.cat([xp.expand(_shift(F, None, -1, ax_cell + 1), ax_sp), F_in,
+                                  xp.expand(_shift(F, 1, None, ax_cell + 1), ax_sp)], ax_sp)
+            M_all[idim] = M_fp
+        if self.viscosity:
+            F_all = self.add_viscosity(M_all, F_all)
         return F_all
+
+    def _interfaces(self, M_fp, idim):
+        """The left and right states at the element interfaces along idim of
+        a flux-point array M_fp (the sp axis of idim holds the nf points):
+        src/sd_boundary.py:70-76 (store_BC, store_interfaces, apply_BC),
+        including a "pressure" side's overwrite of the domain-edge state by
+        its stored boundary state."""
+        nd = self.ndim
+        ax_sp = sp_axis(nd, idim)
+        tax = cell_axis(nd, idim) + 1
+        left_trace = xp.take(M_fp, 0, ax_sp)
+        right_trace = xp.take(M_fp, self.nf - 1, ax_sp)
+        Ncell = self.N[idim]
+        first_l = xp.take(left_trace, 0, tax)
+        last_r = xp.take(right_trace, Ncell - 1, tax)
+        bc = []
+        for side in (0, 1):
+            kind = self.BC[idim][side]
+            if kind == "periodic":
+                v = last_r if side == 0 else first_l
+            elif kind in ("reflective", "gradfree"):
+                v = first_l if side == 0 else last_r
+                if kind == "reflective":
+                    v = xp.stack([v[k] * -1 if k == idim + 1 else v[k] for k in range(self.V)], 0)
+            elif kind in ("ic", "eq", "pressure"):
+                b = self.BC_fp[idim][side]
+                v = (b.expand(first_l.shape) if self.torch_mode
+                     else np.broadcast_to(b, first_l.shape).copy())
+            else:
+                raise TypeError("Undetermined boundary type")
+            bc.append(v)
+        # pressure sides overwrite the edge traces with the stored state
+        if self.BC[idim][0] == "pressure":
+            left_trace = xp.cat([xp.expand(bc[0], tax), _shift(left_trace, 1, None, tax)], tax)
+        if self.BC[idim][1] == "pressure":
+            right_trace = xp.cat([_shift(right_trace, None, -1, tax), xp.expand(bc[1], tax)], tax)
+        ML = xp.cat([xp.expand(bc[0], tax), right_trace], tax)
+        MR = xp.cat([left_trace, xp.expand(bc[1], tax)], tax)
+        return ML, MR
+
+    def _apply_interfaces(self, X, M_fp, idim):
+        """src/sd_boundary.py:19-30: interface values X into the two edge
+        flux points of every cell (edge 0 of cell i <- X[i], edge nf-1 <-
+        X[i+1])."""
+        nd = self.ndim
+        ax_sp = sp_axis(nd, idim)
+        tax = cell_axis(nd, idim) + 1
+        return xp.cat([xp.expand(_shift(X, None, -1, tax), ax_sp), _shift(M_fp, 1, -1, ax_sp),
+                       xp.expand(_shift(X, 1, None, tax), ax_sp)], ax_sp)
+
+    def add_viscosity(self, M_all, F_all):
+        """src/sdader_simulator.py:245-268 with src/hydro.py:172-241: the
+        viscous flux subtracted at every flux point.  Primitives at the flux
+        points take the left state at element interfaces (ML); their
+        gradient at the solution points, interpolated to the flux points of
+        each direction, takes the right state (MR)."""
+        nd = self.ndim
+        W_fp, dW_sp = {}, {}
+        for idim in range(nd):
+            Wf = compute_primitives(M_all[idim], nd, self.gamma)
+            ML, _ = self._interfaces(Wf, idim)
+            W_fp[idim] = self._apply_interfaces(ML, Wf, idim)
+            dW_sp[idim] = apply_axis(self.ops["dfp_to_sp"], W_fp[idim], sp_axis(nd, idim),
+                                     axis_order(idim)) / self.h[idim]
+        out = {}
+        for idim in range(nd):
+            vels = self.rolled_vels(idim)
+            dW_fp = {}
+            for e in range(nd):
+                G = apply_axis(self.ops["sp_to_fp"], dW_sp[e], sp_axis(nd, idim), axis_order(idim))
+                _, MR = self._interfaces(G, idim)
+                dW_fp[e] = self._apply_interfaces(MR, G, idim)
+            out[idim] = F_all[idim] - viscous_fluxes(W_fp[idim], vels, dW_fp, self.nu, self.beta)
+        return out
 
     def ader_dudt(self, F_all):
         """src/sdader_simulator.py:148-158 with src/sd_simulator.py:196-206."""

@@ -69,6 +69,9 @@ class spd_config(ctypes.Structure):
         ("min_P", ctypes.c_double),
         ("godunov", ctypes.c_int),
         ("BC", (ctypes.c_int * 2) * 3),
+        ("viscosity", ctypes.c_int),
+        ("nu", ctypes.c_double),
+        ("beta", ctypes.c_double),
     ]
 
 

@@ -118,6 +118,11 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
     return fail(C, SPD_ERR_ARG, "bad Riemann solver");
   if (cfg->slope_limiter < 0 || cfg->slope_limiter > 1) return fail(C, SPD_ERR_ARG, "bad slope limiter");
   if (cfg->update != SPD_UPDATE_SD && cfg->update != SPD_UPDATE_FV) return fail(C, SPD_ERR_ARG, "bad update");
+  if (cfg->viscosity && cfg->update == SPD_UPDATE_FV && cfg->FB)
+    return fail(C, SPD_ERR_ARG,
+                "viscosity with the FV update and FB: the reference's viscous fallback fluxes raise "
+                "AttributeError (src/muscl.py:253 calls compute_slopes, which calls a missing method)");
+  if (cfg->viscosity && !(cfg->nu >= 0.0)) return fail(C, SPD_ERR_ARG, "nu must be >= 0");
   if (cfg->update == SPD_UPDATE_FV && cfg->FB) {
     // src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros (the
     // perturbation of the well-balanced mode, which is not implemented), so
@@ -179,6 +184,9 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   g.gamma = cfg->gamma;
   g.min_c2 = cfg->min_c2;
   C->h_dt = h_min / (double)(P + 1);
+  // viscous dt limit h**2/nu*.25 (src/sd_simulator.py:223-224); h*h is the
+  // correctly rounded square, as Python's h**2
+  if (cfg->viscosity && cfg->nu > 0.0) C->dt_visc = C->h_dt * C->h_dt / cfg->nu * 0.25;
 
   const int n = C->n, nf = C->nf, T = C->T, V = C->V, NS = C->NS, NJ = C->NJ;
   std::memcpy(C->ops.sp_to_fp, ops->sp_to_fp, sizeof(double) * nf * n);
@@ -270,6 +278,13 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
     if (int r = dalloc(C, &C->Fi[d], (size_t)V * T * NJ * nI)) return r;
     if (int r = dalloc(C, &C->bcfix[d], (size_t)2 * V * NJ * (Nc / g.N[d]))) return r;
     CK(cudaMemset(C->bcfix[d], 0, sizeof(double) * 2 * V * NJ * (Nc / g.N[d])));
+  }
+  if (cfg->viscosity) {
+    if (int r = dalloc(C, &C->dWsp, (size_t)D * V * T * NS * Nc)) return r;
+    for (int d = 0; d < D; ++d) {
+      if (int r = dalloc(C, &C->Wfp[d], (size_t)V * T * NJ * nf * Nc)) return r;
+      if (int r = dalloc(C, &C->Gv[d], (size_t)V * T * NJ * nf * Nc)) return r;
+    }
   }
   if (cfg->update == SPD_UPDATE_FV) {
     if (int r = dalloc(C, &C->U_new, (size_t)V * Nq)) return r;

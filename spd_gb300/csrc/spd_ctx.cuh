@@ -14,6 +14,7 @@
 #include "../../include/spd_gb300.h"
 #include "spd_batch.cuh"
 #include "spd_fv.cuh"
+#include "spd_visc.cuh"
 
 namespace spd_host {
 struct StepperBase;
@@ -84,6 +85,12 @@ struct spd_ctx {
   double* Fi[3] = {nullptr, nullptr, nullptr};
   double* Ffp[3] = {nullptr, nullptr, nullptr};
   double* bcfix[3] = {nullptr, nullptr, nullptr};
+  // viscosity scratch: primitives at the flux points (left interface
+  // states), their gradients at the solution points, viscous fluxes
+  double* Wfp[3] = {nullptr, nullptr, nullptr};
+  double* dWsp = nullptr;
+  double* Gv[3] = {nullptr, nullptr, nullptr};
+  double dt_visc = -1.0;  // h^2 / nu / 4 of the viscous dt limit, or < 0
   // FV scratch
   double* F_HO[3] = {nullptr, nullptr, nullptr};
   double *ext_old = nullptr, *ext_new = nullptr, *theta_src = nullptr, *theta_a = nullptr, *theta_b = nullptr;

@@ -846,19 +846,23 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
 
 // dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when
 // a NaN entered the reduction) (src/sd_simulator.py:214-227)
+// dt = cfl * min(h / c_max, h^2 / nu / 4) (src/sd_simulator.py:214-227; the
+// viscous limit only when dt_visc >= 0; Python's min keeps its first
+// argument unless the second is smaller, so a NaN dt stays NaN)
 struct DtFinal {
   static __device__ __forceinline__ void run(Blk, double h, double cfl, const unsigned long long* cmax_bits,
-                                             const int* nan_flag, double* dt) {
+                                             const int* nan_flag, double* dt, double dt_visc) {
     if (threadIdx.x != 0) return;
     const double cmax = *nan_flag ? __longlong_as_double(0x7ff8000000000000LL)
                                   : __longlong_as_double((long long)*cmax_bits);
-    const double dtt = h / cmax;
+    double dtt = h / cmax;
+    if (dt_visc >= 0.0 && dt_visc < dtt) dtt = dt_visc;
     *dt = cfl * dtt;
   }
 };
 static __global__ void k_dt_final(double h, double cfl, const unsigned long long* cmax_bits, const int* nan_flag,
-                           double* dt) {
-  DtFinal::run(hw_blk(), h, cfl, cmax_bits, nan_flag, dt);
+                           double* dt, double dt_visc) {
+  DtFinal::run(hw_blk(), h, cfl, cmax_bits, nan_flag, dt, dt_visc);
 }
 
 }  // namespace spd

@@ -251,14 +251,20 @@ __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double
 // mode: 0 = Picard (writes U_ader and next traces), 1 = SD update of U_sp,
 //       2 = write Ffp.
 // ---------------------------------------------------------------------------
-template <int D, int P>
+// VISC: the viscous fluxes G[d] (src/sdader_simulator.py:268, layout of
+// Ffp) are subtracted from the flux at every flux point, Riemann edges
+// included, before the derivative (spd_visc.cuh).
+template <int D, int P, bool VISC = false>
 struct Interior {
 static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int mode, int Teff,
                                            const double* __restrict__ Uin, int Tu, const double* __restrict__ dt_ptr,
                                            double* __restrict__ U_sp, double* __restrict__ U_ader, const double* Fi0,
                                            const double* Fi1, const double* Fi2, double* tr0, double* tr1,
-                                           double* tr2, double* Ffp0, double* Ffp1, double* Ffp2) {
+                                           double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
+                                           const double* G0 = nullptr, const double* G1 = nullptr,
+                                           const double* G2 = nullptr) {
   using k = K<D, P>;
+  const double* Gv[3] = {G0, G1, G2};
   extern __shared__ double dudt_s[];  // [(v*NS + s)*Teff + tl][CPB]
   const int CPB = blockDim.x;
   const int cl = threadIdx.x, tl = threadIdx.y;
@@ -298,6 +304,13 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
         for (int v = 0; v < k::V; ++v) {
           Fl[v][0] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + il];
           Fl[v][k::nf - 1] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + ir];
+        }
+        if (VISC) {
+#pragma unroll
+          for (int v = 0; v < k::V; ++v)
+#pragma unroll
+            for (int f = 0; f < k::nf; ++f)
+              Fl[v][f] = Fl[v][f] - Gv[d][((((long long)v * g.T + tl) * k::NJ + j) * k::nf + f) * g.Nc + c];
         }
         if (mode == 2) {
 #pragma unroll
@@ -361,6 +374,27 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
                            double* tr2, double* Ffp0, double* Ffp1, double* Ffp2) {
   Interior<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2, Ffp0,
                       Ffp1, Ffp2);
+}
+template <int D, int P>
+struct InteriorVisc {
+  static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int mode, int Teff,
+                                             const double* __restrict__ Uin, int Tu, const double* __restrict__ dt_ptr,
+                                             double* __restrict__ U_sp, double* __restrict__ U_ader,
+                                             const double* Fi0, const double* Fi1, const double* Fi2, double* tr0,
+                                             double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
+                                             const double* G0, const double* G1, const double* G2) {
+    Interior<D, P, true>::run(B, op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2, Ffp0,
+                              Ffp1, Ffp2, G0, G1, G2);
+  }
+};
+template <int D, int P>
+__global__ void k_interior_visc(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
+                                const double* __restrict__ dt_ptr, double* __restrict__ U_sp,
+                                double* __restrict__ U_ader, const double* Fi0, const double* Fi1, const double* Fi2,
+                                double* tr0, double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
+                                const double* G0, const double* G1, const double* G2) {
+  InteriorVisc<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2,
+                          Ffp0, Ffp1, Ffp2, G0, G1, G2);
 }
 
 // ---------------------------------------------------------------------------

@@ -75,6 +75,7 @@ struct Stepper : StepperBase {
     cpb = std::min(32, max_cpb);
     smem = per_cell * max_cpb;
     CK(cudaFuncSetAttribute(k_interior<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_interior_visc<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
   }
 
@@ -125,13 +126,37 @@ struct Stepper : StepperBase {
       const int mode = (it < m) ? 0 : final_mode;
       const double* Uin = (it == 0) ? C->U_sp : C->U_ader;
       const int Tu = (it == 0) ? 1 : C->T;
+      const bool visc = C->cfg.viscosity != 0;
+      if (visc) {
+        // viscous fluxes of this iteration (src/sdader_simulator.py:239-268)
+        {
+          ProfScope ps_(C, "k_visc_grad");
+          launch<ViscGrad<D, P>>(C, "k_visc_grad", k_visc_grad<D, P>, blocks_for(g.Nc * Teff, 128), 128, 0, C->ops,
+                                 g, Teff, Uin, Tu, C->trace[0], C->trace[1], C->trace[2], C->bcfix[0], C->bcfix[1],
+                                 C->bcfix[2], C->Wfp[0], C->Wfp[1], C->Wfp[2], C->dWsp);
+        }
+        CKL();
+        {
+          ProfScope ps_(C, "k_visc_flux");
+          launch<ViscFlux<D, P>>(C, "k_visc_flux", k_visc_flux<D, P>, blocks_for(g.Nc * Teff, 128), 128, 0, C->ops,
+                                 g, Teff, C->dWsp, C->Wfp[0], C->Wfp[1], C->Wfp[2], C->bcfix[0], C->bcfix[1],
+                                 C->bcfix[2], C->cfg.nu, C->cfg.beta, C->Gv[0], C->Gv[1], C->Gv[2]);
+        }
+        CKL();
+      }
       // the first Picard iteration computes one time node but writes all T:
       // T thread rows share its output (whole warps per row when cpb is a
       // multiple of 32)
       const int rows = (mode == 0 && Teff == 1 && cpb % 32 == 0) ? C->T : Teff;
       dim3 block(cpb, rows);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
-      {
+      if (visc) {
+        ProfScope ps_(C, "k_interior");
+        launch<InteriorVisc<D, P>>(C, "k_interior", k_interior_visc<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops,
+                                   g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2],
+                                   C->trace[0], C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2], C->Gv[0],
+                                   C->Gv[1], C->Gv[2]);
+      } else {
         ProfScope ps_(C, "k_interior");
         launch<Interior<D, P>>(C, "k_interior", k_interior<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops, g, mode,
                                Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2], C->trace[0],
@@ -181,7 +206,7 @@ struct Stepper : StepperBase {
     {
       ProfScope ps_(C, "k_dt_final");
       launch<DtFinal>(C, "k_dt_final", k_dt_final, 1, 1, 0, C->h_dt, C->cfg.cfl_coeff, C->counts + 2, C->flags + 1,
-                      C->dt);
+                      C->dt, C->dt_visc);
     }
     CKL();
     return 0;

@@ -319,14 +319,14 @@ class SD_Simulator(Simulator):
     GPU.  Constructed on its own it steps with the SD update and no
     limiter; SDADER_Simulator (its subclass) adds the options of the
     reference's SDADER class.  Options the GPU step does not implement
-    (viscosity, potential, WB, isothermal, predictor=False) raise
+    (potential, WB, isothermal, predictor=False, and viscosity with the FV
+    update and FB, which fails in the reference itself) raise
     NotImplementedError here, before any device work.
     """
 
     def __init__(self, riemann_solver_sd: str = "llf", update: str = "SD", *args, **kwargs):
         super().__init__(*args, **kwargs)
-        for flag, name in ((self.isothermal, "isothermal"), (self.viscosity, "viscosity"),
-                           (self.potential, "potential"), (self.WB, "WB")):
+        for flag, name in ((self.isothermal, "isothermal"), (self.potential, "potential"), (self.WB, "WB")):
             if flag:
                 raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
         # options of the classes below SD_Simulator in the reference's chain
@@ -356,6 +356,14 @@ class SD_Simulator(Simulator):
                 "BC 'eq' with update='FV' and FB=True: the reference's fallback fluxes at those boundaries are "
                 "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
                 "first two steps; this combination is refused instead of reproducing a NaN state")
+        if self.viscosity and update == "FV" and self.FB:
+            # src/fv_simulator.py:186-187 -> src/muscl.py:253 -> src/fv_simulator.py:74
+            # -> src/muscl.py:97 calls Slope_limiter.compute_gradient, which does
+            # not exist: the reference's first step with these options raises
+            raise NotImplementedError(
+                "viscosity=True with update='FV' and FB=True: the reference's viscous fallback fluxes raise "
+                "AttributeError ('Slope_limiter' object has no attribute 'compute_gradient'); viscosity runs with "
+                "the SD update or the FV update without FB")
         self.riemann_solver_sd_name = riemann_solver_sd
         self.update = update
         p, m, ndim = self.p, self.m, self.ndim
@@ -474,6 +482,9 @@ class SD_Simulator(Simulator):
         cfg.max_rho = self.max_rho
         cfg.min_P = self.min_P
         cfg.godunov = int(bool(self.godunov))
+        cfg.viscosity = int(bool(self.viscosity))
+        cfg.nu = float(self.nu)
+        cfg.beta = float(self.beta)
         faces = [self.faces[DIMS[i]] for i in range(self.ndim)]
         self._ctx = _lib.Context(cfg, self.ops, faces, variant="fma" if self.fma else "ieee")
 
@@ -722,7 +733,8 @@ class SD_Simulator(Simulator):
                     FB=bool(self.FB), riemann_solver_sd=self.riemann_solver_sd_name,
                     riemann_solver_fv=self.riemann_solver_fv_name, slope_limiter=self.slope_limiter_name,
                     BC=[list(self.BC[d]) for d in self.dims], gamma=self.gamma, cfl_coeff=self.cfl_coeff,
-                    lims=[list(self.lim[d]) for d in self.dims])
+                    lims=[list(self.lim[d]) for d in self.dims], viscosity=bool(self.viscosity), nu=self.nu,
+                    beta=self.beta)
 
     def save_state(self, path) -> None:
         """Write U_sp, U_cv, W_cv, the FV boundary buffers, time, n_step, dt

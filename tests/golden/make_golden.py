@@ -61,6 +61,26 @@ CASES = {
                                             riemann_solver_sd="hllc", riemann_solver_fv="llf",
                                             BC=(("gradfree", "reflective"), ("periodic", "periodic"))),
                                        ("four_quadrant", {}), 3),
+    # viscosity (src/sdader_simulator.py:245-268): SD update and the FV
+    # update without limiting (with FB=True the reference's viscous fallback
+    # fluxes raise AttributeError, src/muscl.py:253, src/muscl.py:97)
+    "visc_sine8_p2_sd_llf_periodic_dtclamp": (dict(p=2, N=(8, 8), update="SD", riemann_solver_sd="llf",
+                                                   viscosity=True, nu=0.05,
+                                                   BC=(("periodic", "periodic"),) * 2),
+                                              ("sine_wave", {}), 6),
+    "visc_kh16_p3_fv_hllc_periodic": (dict(p=3, N=(16, 16), update="FV", FB=False, riemann_solver_sd="hllc",
+                                           viscosity=True, nu=1e-3, BC=(("periodic", "periodic"),) * 2),
+                                      ("kelvin_helmholtz", {"N": 16}), 4),
+    "visc_quadrant8_p2_sd_hllc_mixed_bc": (dict(p=2, N=(8, 8), update="SD", riemann_solver_sd="hllc",
+                                                viscosity=True, nu=2e-3, beta=0.5,
+                                                BC=(("reflective", "gradfree"), ("ic", "pressure"))),
+                                           ("four_quadrant", {}), 4),
+    "visc_sedov4_p2_fv_llf_reflective_3d": (dict(p=2, N=(4, 4, 4), update="FV", riemann_solver_sd="llf",
+                                                 viscosity=True, nu=1e-3,
+                                                 BC=(("reflective", "reflective"),) * 3),
+                                            ("sedov", {"N": 4}), 3),
+    "visc_sod16_p3_sd_llf_eq": (dict(p=3, N=(16,), update="SD", riemann_solver_sd="llf", viscosity=True, nu=1e-3,
+                                     BC=(("eq", "eq"),)), ("sod", {}), 5),
 }
 
 
@@ -92,6 +112,9 @@ LONG_CASES = {
     "sod64_p2_fvfb_llf_gradfree_t02": (dict(p=2, N=(64,), update="FV", FB=True, riemann_solver_sd="llf",
                                             riemann_solver_fv="llf", BC=(("gradfree", "gradfree"),)),
                                        ("sod", {}), {"t_end": 0.2}),
+    "visc_kh32_p3_sd_hllc_periodic_100steps": (dict(p=3, N=(32, 32), update="SD", riemann_solver_sd="hllc",
+                                                    viscosity=True, nu=1e-3, BC=(("periodic", "periodic"),) * 2),
+                                               ("kelvin_helmholtz", {"N": 32}), {"steps": 100}),
     "step16_p3_sd_hllc_periodic_100steps": (dict(p=3, N=(16, 16), update="SD", riemann_solver_sd="hllc",
                                                  BC=(("periodic", "periodic"),) * 2),
                                             ("step_function", {}), {"steps": 100}),

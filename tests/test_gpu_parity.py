@@ -200,3 +200,42 @@ def test_options_vs_oracle(name):
                       "sod": ics.sod, "sedov4": ics.sedov(4)}[init]
     bad, _ = _run_vs_oracle(3, **kw)
     assert not bad, bad
+
+
+VISC_CASES = {
+    "2d_fv_nofb_gradfree_reflective": dict(p=3, N=(10, 8), init="four_quadrant", update="FV", FB=False,
+                                           riemann_solver_sd="hllc", viscosity=True, nu=1e-3,
+                                           BC=(("gradfree", "reflective"), ("reflective", "gradfree"))),
+    "3d_sd_periodic_pressure": dict(p=2, N=(4, 5, 3), init="sedov4", update="SD", riemann_solver_sd="llf",
+                                    viscosity=True, nu=2e-3, beta=0.25,
+                                    BC=(("periodic", "periodic"), ("pressure", "ic"), ("reflective", "eq"))),
+    "1d_sd_m2_p4": dict(p=4, m=2, N=(12,), init="sod", update="SD", riemann_solver_sd="lhllc", viscosity=True,
+                        nu=1e-2, BC=(("gradfree", "gradfree"),)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(VISC_CASES))
+def test_viscosity_vs_oracle(name):
+    """The viscous predictor (src/sdader_simulator.py:245-268) on further
+    boundary mixes, degrees and time orders, 3 steps, bitwise."""
+    from spd_gb300 import initial_conditions as ics
+    kw = dict(VISC_CASES[name])
+    init = kw.pop("init")
+    kw["init_fct"] = {"four_quadrant": ics.four_quadrant, "sod": ics.sod, "sedov4": ics.sedov(4)}[init]
+    from spd_gb300 import SDADER_Simulator
+    s = SDADER_Simulator(verbose=False, **kw)
+    o = oracle_like(s, viscosity=True, nu=kw["nu"], beta=kw.get("beta", 2.0 / 3))
+    dts = step_both(s, o, 3)
+    assert all(a == b for a, b in dts), dts
+    assert not compare(s, o)
+    s.close()
+
+
+def test_viscosity_refused_where_the_reference_fails():
+    from spd_gb300 import SDADER_Simulator
+    with pytest.raises(NotImplementedError, match="compute_gradient"):
+        SDADER_Simulator(N=(4, 4), update="FV", FB=True, viscosity=True, verbose=False)
+    s = SDADER_Simulator(N=(4, 4), update="SD", viscosity=True, verbose=False)
+    with pytest.raises(Exception, match="viscous"):
+        s._ctx.adjoint_enable(1)
+    s.close()
