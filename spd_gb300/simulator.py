@@ -606,7 +606,7 @@ class SD_Simulator(Simulator):
             fid = fid + np.moveaxis(coord.reshape(coord.shape + (1,) * (2 * nd - 2)), [0, 1],
                                     [nd - 1 - i, 2 * nd - 1 - i]).reshape(shp) * stride
             stride *= FX[i]
-        return raw[:, :, fid].transpose((1, 0) + tuple(range(2, 2 + 2 * nd)))
+        return np.ascontiguousarray(raw[:, :, fid].transpose((1, 0) + tuple(range(2, 2 + 2 * nd))))
 
     def transpose_to_fv(self, M):
         if self.ndim == 1:

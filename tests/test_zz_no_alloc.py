@@ -72,16 +72,22 @@ def test_cfl_dt_noalloc_partial_last_block_and_nan():
         assert rc == 0
         torch.cuda.synchronize()
         assert out.item() == expected, (call, out.item(), expected)
-    W_sd = s.dm.W_cv
-    W_sd[0, 17, 3, 1, 2] = np.nan  # one subcell's density (SD layout)
-    s.dm.W_cv = W_sd
-    s.compute_dt()
-    assert math.isnan(s.dm.dt)
-    W = torch.from_numpy(np.ascontiguousarray(s.transpose_to_fv(W_sd))).cuda()
-    rc = fn(W.data_ptr(), W[0].numel(), s.ndim, s.gamma, s.min_c2, s.cfl_coeff, h, out.data_ptr(), stream)
-    assert rc == 0
-    torch.cuda.synchronize()
-    assert math.isnan(out.item())
+    # a NaN density or pressure becomes the sound-speed floor (np.where(c2 >
+    # min_c2, c2, min_c2) keeps min_c2 for NaN, src/hydro.py:3-25): dt stays
+    # finite and equal; a NaN velocity reaches the maximum and dt is NaN
+    for var, want_nan in ((0, False), (1, True)):
+        W_sd = s.dm.W_cv
+        W_sd[var, 17, 3, 1, 2] = np.nan  # one subcell (SD layout)
+        s.dm.W_cv = W_sd
+        s.compute_dt()
+        expected = s.dm.dt
+        assert math.isnan(expected) == want_nan
+        W = torch.from_numpy(np.ascontiguousarray(s.transpose_to_fv(W_sd))).cuda()
+        rc = fn(W.data_ptr(), W[0].numel(), s.ndim, s.gamma, s.min_c2, s.cfl_coeff, h, out.data_ptr(), stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        got = out.item()
+        assert (math.isnan(got) and want_nan) or got == expected, (var, got, expected)
     s.close()
 
 
