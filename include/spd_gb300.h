@@ -80,7 +80,14 @@ enum spd_field {
    * x-fastest with N_d*(p+1)+1 faces along d and N*(p+1) along the others */
   SPD_F_FACES_X = 15,
   SPD_F_FACES_Y = 16,
-  SPD_F_FACES_Z = 17
+  SPD_F_FACES_Z = 17,
+  /* write-only, with potential: the gravity potential's gradient
+   * (src/sdader_simulator.py:425-434) at the solution points, (ndim, Nz, Ny,
+   * Nx, nz, ny, nx), and its subcell averages in the same SD layout
+   * (compute_cv_from_sp of the former; the reference keeps them transposed
+   * to the FV layout) */
+  SPD_GRAD_PHI_SP = 18,
+  SPD_GRAD_PHI_CV = 19
 };
 
 /* Constructor options of SDADER_Simulator (src/simulator.py:10-36,
@@ -114,6 +121,9 @@ typedef struct spd_config {
   int viscosity;
   double nu;
   double beta;
+  /* gravity potential source terms (src/simulator.py:197-203) in the
+   * predictor's dUdt and the subcell update; gradients by spd_upload */
+  int potential;
 } spd_config;
 
 /* Constant operators built at setup on the host

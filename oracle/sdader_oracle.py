@@ -502,7 +502,7 @@ class OracleSDADER:
     def __init__(self, *, ndim, N, p, m, lims, BC, gamma, cfl_coeff, min_c2,
                  riemann_solver_sd, riemann_solver_fv, slope_limiter, update,
                  FB, tolerance, SED, NAD, PAD, blending, min_rho, max_rho,
-                 min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3):
+                 min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3, potential=False):
         self.ndim = ndim
         self.N = list(N)          # cells per dim, x first
         self.p = p
@@ -532,6 +532,7 @@ class OracleSDADER:
         self.viscosity = viscosity
         self.nu = nu
         self.beta = beta
+        self.potential = potential
         self.ngh = Nghc
         self.ops = {k: (_Mat(v) if k in ("sp_to_fp", "dfp_to_sp", "sp_to_cv", "cv_to_sp", "invader", "w_tp")
                         else v) for k, v in ops.items()}
@@ -550,6 +551,12 @@ class OracleSDADER:
         self.U_sp = conv(state["U_sp"])
         self.U_cv = conv(state["U_cv"])
         self.W_cv = conv(state["W_cv"])
+        # gravity potential gradients (src/sdader_simulator.py:425-434): at
+        # the solution points (ndim, cells..., points...) and as subcell
+        # averages in the FV layout (ndim, subcells...)
+        if potential:
+            self.grad_phi_sp = conv(state["grad_phi_sp"])
+            self.grad_phi_fv = conv(state["grad_phi_fv"])
         self.BC_fp = {i: conv(state[f"BC_fp_{DIMS[i]}"]) for i in range(ndim) if f"BC_fp_{DIMS[i]}" in state}
         self.BC_fv = {}
         for i in range(ndim):
@@ -708,14 +715,28 @@ class OracleSDADER:
             out[idim] = F_all[idim] - viscous_fluxes(W_fp[idim], vels, dW_fp, self.nu, self.beta)
         return out
 
-    def ader_dudt(self, F_all):
+    def ader_dudt(self, F_all, U_ader):
         """src/sdader_simulator.py:148-158 with src/sd_simulator.py:196-206."""
         dUdt = None
         for idim in range(self.ndim):
             part = apply_axis(self.ops["dfp_to_sp"], F_all[idim], sp_axis(self.ndim, idim),
                               axis_order(idim)) / self.h[idim]
             dUdt = part if dUdt is None else dUdt + part
+        if self.potential:
+            dUdt = self.apply_potential(dUdt, U_ader, xp.expand(self.grad_phi_sp, 1))
         return dUdt
+
+    def apply_potential(self, dUdt, U, grad_phi):
+        """src/simulator.py:197-203: the gravity source, dUdt[vel] += rho *
+        dphi/dx_vel and dUdt[P] += m_vel * dphi/dx_vel, direction by
+        direction."""
+        comp = [dUdt[v] for v in range(self.V)]
+        _p_ = self.ndim + 1
+        for idim in range(self.ndim):
+            vel = idim + 1
+            comp[vel] = comp[vel] + U[0] * grad_phi[idim]
+            comp[_p_] = comp[_p_] + U[vel] * grad_phi[idim]
+        return xp.stack(comp, 0)
 
     def ader_predictor(self):
         """src/sdader_simulator.py:160-200; returns the last F_ader_fp."""
@@ -725,8 +746,9 @@ class OracleSDADER:
         F_all = None
         for it in range(self.m + 1):
             F_all = self.solve_faces(U_ader)
+            self.U_ader = U_ader
             if it < self.m:
-                dudt = self.ader_dudt(F_all)
+                dudt = self.ader_dudt(F_all, U_ader)
                 cols = [dudt[:, pp] for pp in range(T)]
                 terms_n = [_sum_terms([inv[nn, pp] * cols[pp] for pp in range(T)], "seq") for nn in range(T)]
                 upd = xp.stack(terms_n, 1) * self.dt
@@ -736,7 +758,7 @@ class OracleSDADER:
 
     def ader_update(self, F_all):
         """src/sdader_simulator.py:202-208."""
-        dudt = self.ader_dudt(F_all)
+        dudt = self.ader_dudt(F_all, self.U_ader)
         w = self.ops["w_tp"]
         dUdt = _sum_terms([w[t] * dudt[:, t] for t in range(self.T)], "seq") * self.dt
         self.U_sp = self.U_sp - dUdt
@@ -860,6 +882,8 @@ class OracleSDADER:
             ax = self.ndim - idim
             part = (_shift(F[idim], 1, None, ax) - _shift(F[idim], None, -1, ax)) / dx
             dUdt = part if dUdt is None else dUdt + part
+        if self.potential:
+            dUdt = self.apply_potential(dUdt, U_cv, self.grad_phi_fv)
         return U_cv - dUdt * dt
 
     def detect_troubles(self, U_cv, U_new):

@@ -27,6 +27,7 @@ FIELD = {
     "BC_fp_x": 8, "BC_fp_y": 9, "BC_fp_z": 10,
     "BC_fv_x": 11, "BC_fv_y": 12, "BC_fv_z": 13, "U_sp_adj": 14,
     "F_faces_x": 15, "F_faces_y": 16, "F_faces_z": 17,
+    "grad_phi_sp": 18, "grad_phi_cv": 19,
 }
 
 # every entry point declared in include/spd_gb300.h
@@ -72,6 +73,7 @@ class spd_config(ctypes.Structure):
         ("viscosity", ctypes.c_int),
         ("nu", ctypes.c_double),
         ("beta", ctypes.c_double),
+        ("potential", ctypes.c_int),
     ]
 
 

@@ -279,6 +279,12 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
     if (int r = dalloc(C, &C->bcfix[d], (size_t)2 * V * NJ * (Nc / g.N[d]))) return r;
     CK(cudaMemset(C->bcfix[d], 0, sizeof(double) * 2 * V * NJ * (Nc / g.N[d])));
   }
+  if (cfg->potential) {
+    if (int r = dalloc(C, &C->gphi_sp, (size_t)D * NS * Nc)) return r;
+    if (int r = dalloc(C, &C->gphi_fv, (size_t)D * Nq)) return r;
+    CK(cudaMemset(C->gphi_sp, 0, sizeof(double) * D * NS * Nc));
+    CK(cudaMemset(C->gphi_fv, 0, sizeof(double) * D * Nq));
+  }
   if (cfg->viscosity) {
     if (int r = dalloc(C, &C->dWsp, (size_t)D * V * T * NS * Nc)) return r;
     for (int d = 0; d < D; ++d) {
@@ -438,6 +444,8 @@ static size_t field_count(spd_ctx* C, int field) {
       const int d = field - SPD_BC_FV_X;
       return d < D ? (size_t)2 * V * NGH * n_other_ext(g, d) : 0;
     }
+    case SPD_GRAD_PHI_SP:
+    case SPD_GRAD_PHI_CV: return C->gphi_sp ? (size_t)D * C->NS * g.Nc : 0;
     case SPD_F_FACES_X:
     case SPD_F_FACES_Y:
     case SPD_F_FACES_Z: {
@@ -483,6 +491,18 @@ int spd_upload(spd_ctx* C, int field, const double* host, size_t count) {
                   : (field == SPD_U_CV ? C->U_cv : (field == SPD_W_CV ? C->W_cv : C->Usp_a));
     k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, C->staging, dst, 1,
                                                                        (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
+    CKL();
+    CK(cudaStreamSynchronize(C->stream));
+    return SPD_OK;
+  }
+  if (field == SPD_GRAD_PHI_SP || field == SPD_GRAD_PHI_CV) {
+    // ndim components in the SD layout: to [d][s][cell] (solution points)
+    // or the FV layout [d][subcell] (subcell averages)
+    if (int r = ensure_staging(C, need)) return r;
+    CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyDefault, C->stream));
+    double* dst = (field == SPD_GRAD_PHI_SP) ? C->gphi_sp : C->gphi_fv;
+    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->D, C->staging, dst, 1,
+                                                                       field == SPD_GRAD_PHI_SP ? 0 : 1);
     CKL();
     CK(cudaStreamSynchronize(C->stream));
     return SPD_OK;

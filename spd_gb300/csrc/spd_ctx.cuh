@@ -91,6 +91,10 @@ struct spd_ctx {
   double* dWsp = nullptr;
   double* Gv[3] = {nullptr, nullptr, nullptr};
   double dt_visc = -1.0;  // h^2 / nu / 4 of the viscous dt limit, or < 0
+  // gravity potential gradients: [d][s][cell] at the solution points and
+  // [d][subcell] as subcell averages (FV layout)
+  double* gphi_sp = nullptr;
+  double* gphi_fv = nullptr;
   // FV scratch
   double* F_HO[3] = {nullptr, nullptr, nullptr};
   double *ext_old = nullptr, *ext_new = nullptr, *theta_src = nullptr, *theta_a = nullptr, *theta_b = nullptr;

@@ -75,6 +75,20 @@ __device__ __forceinline__ bool gt0_key(double x) {
   return b > 0 && b <= 0x7ff0000000000000LL;
 }
 
+// gravity source of one subcell (src/fv_simulator.py:200-203 with
+// src/simulator.py:197-203): dUdt[vel] += rho * dphi_vel, dUdt[P] +=
+// m_vel * dphi_vel, direction by direction; gphi [d][subcell]
+template <int D>
+__device__ __forceinline__ void potential_source(const Geo& g, const double* __restrict__ gphi, long long q,
+                                                 const double* u, double* dudt) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double gp = gphi[(long long)d * g.Nq + q];
+    dudt[d + 1] = dudt[d + 1] + u[0] * gp;
+    dudt[D + 1] = dudt[D + 1] + u[d + 1] * gp;
+  }
+}
+
 // dUdt of one subcell from the face fluxes (src/fv_simulator.py:189-205)
 template <int D>
 __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, int ix, int iy, int iz,
@@ -106,7 +120,8 @@ struct FvCandidate {
 static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg, const double* __restrict__ dt_ptr,
                                            double w_i, const double* F0, const double* F1, const double* F2,
                                            const double* __restrict__ U_cv, double* __restrict__ U_new,
-                                           double* ext_old, double* ext_new, int write_ext) {
+                                           double* ext_old, double* ext_new, int write_ext,
+                                           const double* __restrict__ gphi) {
   constexpr int V = D + 2;
   const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nq) return;
@@ -114,14 +129,15 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
   q_coords(g, q, ix, iy, iz);
   const double* F[3] = {F0, F1, F2};
   const double dti = *dt_ptr * w_i;
-  double u[V], un[V];
+  double u[V], un[V], dudt[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
 #pragma unroll
+  for (int v = 0; v < V; ++v) flux_divergence<D>(g, fg, ix, iy, iz, F, v, dudt[v]);
+  if (gphi != nullptr) potential_source<D>(g, gphi, q, u, dudt);
+#pragma unroll
   for (int v = 0; v < V; ++v) {
-    double dudt;
-    flux_divergence<D>(g, fg, ix, iy, iz, F, v, dudt);
-    un[v] = u[v] - dudt * dti;
+    un[v] = u[v] - dudt[v] * dti;
     U_new[(long long)v * g.Nq + q] = un[v];
   }
   if (write_ext) {
@@ -145,8 +161,8 @@ template <int D>
 __global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i,
                                const double* F0, const double* F1, const double* F2,
                                const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
-                               double* ext_new, int write_ext) {
-  FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext);
+                               double* ext_new, int write_ext, const double* __restrict__ gphi) {
+  FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext, gphi);
 }
 
 // W_cv (subcell layout) from the active region of an extended primitive
@@ -783,7 +799,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
                                            const double* F1, const double* F2, const double* B0, const double* B1,
                                            const double* B2, const double* A0, const double* A1, const double* A2,
                                            const double* __restrict__ U_cv, double* __restrict__ U_new,
-                                           double* __restrict__ ext_new) {
+                                           double* __restrict__ ext_new, const double* __restrict__ gphi) {
   constexpr int V = D + 2;
   const unsigned long long cnt = *count;
   const double* FH[3] = {F0, F1, F2};
@@ -796,9 +812,10 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
   int ix, iy, iz;
   q_coords(g, q, ix, iy, iz);
   const int ii[3] = {ix, iy, iz};
-  double un[V];
+  double un[V], dudt[V], u[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) {
+    u[v] = U_cv[(long long)v * g.Nq + q];
     double acc = 0.0;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -817,7 +834,12 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
       const double part = div_rcp(Fv[1] - Fv[0], fg.dx[d][ii[d]], fg.rdx[d][ii[d]]);
       acc = (d == 0) ? part : acc + part;
     }
-    un[v] = U_cv[(long long)v * g.Nq + q] - acc * dti;
+    dudt[v] = acc;
+  }
+  if (gphi != nullptr) potential_source<D>(g, gphi, q, u, dudt);
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    un[v] = u[v] - dudt[v] * dti;
     U_new[(long long)v * g.Nq + q] = un[v];
   }
   if (ext_new != nullptr) {
@@ -839,9 +861,9 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
                              const double* F0, const double* F1, const double* F2, const double* B0,
                              const double* B1, const double* B2, const double* A0, const double* A1,
                              const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new,
-                             double* __restrict__ ext_new) {
+                             double* __restrict__ ext_new, const double* __restrict__ gphi) {
   FvCorrect<D>::run(hw_blk(), g, fg, dt_ptr, w_i, godunov, list, count, F0, F1, F2, B0, B1, B2, A0, A1, A2, U_cv,
-                    U_new, ext_new);
+                    U_new, ext_new, gphi);
 }
 
 // dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when

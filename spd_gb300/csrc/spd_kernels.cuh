@@ -251,10 +251,13 @@ __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double
 // mode: 0 = Picard (writes U_ader and next traces), 1 = SD update of U_sp,
 //       2 = write Ffp.
 // ---------------------------------------------------------------------------
-// VISC: the viscous fluxes G[d] (src/sdader_simulator.py:268, layout of
-// Ffp) are subtracted from the flux at every flux point, Riemann edges
-// included, before the derivative (spd_visc.cuh).
-template <int D, int P, bool VISC = false>
+// EXT: optional terms, each present when its pointer is not null -- the
+// viscous fluxes G[d] (src/sdader_simulator.py:268, layout of Ffp),
+// subtracted from the flux at every flux point, Riemann edges included,
+// before the derivative (spd_visc.cuh); the gravity source of the
+// potential gradient gphi [d][s][cell] added to the derivative
+// (src/sdader_simulator.py:154-157, src/simulator.py:197-203).
+template <int D, int P, bool EXT = false>
 struct Interior {
 static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int mode, int Teff,
                                            const double* __restrict__ Uin, int Tu, const double* __restrict__ dt_ptr,
@@ -262,9 +265,11 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
                                            const double* Fi1, const double* Fi2, double* tr0, double* tr1,
                                            double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
                                            const double* G0 = nullptr, const double* G1 = nullptr,
-                                           const double* G2 = nullptr) {
+                                           const double* G2 = nullptr, const double* gphi = nullptr) {
   using k = K<D, P>;
   const double* Gv[3] = {G0, G1, G2};
+  const bool visc = EXT && G0 != nullptr;
+  const bool pot = EXT && gphi != nullptr;
   extern __shared__ double dudt_s[];  // [(v*NS + s)*Teff + tl][CPB]
   const int CPB = blockDim.x;
   const int cl = threadIdx.x, tl = threadIdx.y;
@@ -305,7 +310,7 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
           Fl[v][0] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + il];
           Fl[v][k::nf - 1] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + ir];
         }
-        if (VISC) {
+        if (visc) {
 #pragma unroll
           for (int v = 0; v < k::V; ++v)
 #pragma unroll
@@ -332,6 +337,22 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
               *slot = (d == 0) ? val : *slot + val;
             }
           }
+        }
+      }
+    }
+    if (pot && mode != 2) {
+      // dUdt[vel] += rho * dphi_vel, dUdt[P] += m_vel * dphi_vel, direction by
+      // direction, with the iterate the fluxes came from
+      for (int s = 0; s < k::NS; ++s) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double gp = gphi[((long long)d * k::NS + s) * g.Nc + c];
+          const double u0 = Uin[(((long long)0 * Tu + tu) * k::NS + s) * g.Nc + c];
+          const double uv = Uin[(((long long)(d + 1) * Tu + tu) * k::NS + s) * g.Nc + c];
+          double* sv = &dudt_s[((((long long)(d + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
+          *sv = *sv + u0 * gp;
+          double* sp = &dudt_s[((((long long)(D + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
+          *sp = *sp + uv * gp;
         }
       }
     }
@@ -376,25 +397,26 @@ __global__ void k_interior(Ops op, Geo g, int mode, int Teff, const double* __re
                       Ffp1, Ffp2);
 }
 template <int D, int P>
-struct InteriorVisc {
+struct InteriorExt {
   static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, int mode, int Teff,
                                              const double* __restrict__ Uin, int Tu, const double* __restrict__ dt_ptr,
                                              double* __restrict__ U_sp, double* __restrict__ U_ader,
                                              const double* Fi0, const double* Fi1, const double* Fi2, double* tr0,
                                              double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
-                                             const double* G0, const double* G1, const double* G2) {
+                                             const double* G0, const double* G1, const double* G2,
+                                             const double* gphi) {
     Interior<D, P, true>::run(B, op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2, Ffp0,
-                              Ffp1, Ffp2, G0, G1, G2);
+                              Ffp1, Ffp2, G0, G1, G2, gphi);
   }
 };
 template <int D, int P>
-__global__ void k_interior_visc(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
-                                const double* __restrict__ dt_ptr, double* __restrict__ U_sp,
-                                double* __restrict__ U_ader, const double* Fi0, const double* Fi1, const double* Fi2,
-                                double* tr0, double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
-                                const double* G0, const double* G1, const double* G2) {
-  InteriorVisc<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2,
-                          Ffp0, Ffp1, Ffp2, G0, G1, G2);
+__global__ void k_interior_ext(Ops op, Geo g, int mode, int Teff, const double* __restrict__ Uin, int Tu,
+                               const double* __restrict__ dt_ptr, double* __restrict__ U_sp,
+                               double* __restrict__ U_ader, const double* Fi0, const double* Fi1, const double* Fi2,
+                               double* tr0, double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
+                               const double* G0, const double* G1, const double* G2, const double* gphi) {
+  InteriorExt<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2,
+                         Ffp0, Ffp1, Ffp2, G0, G1, G2, gphi);
 }
 
 // ---------------------------------------------------------------------------

@@ -75,7 +75,7 @@ struct Stepper : StepperBase {
     cpb = std::min(32, max_cpb);
     smem = per_cell * max_cpb;
     CK(cudaFuncSetAttribute(k_interior<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_interior_visc<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_interior_ext<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
   }
 
@@ -150,12 +150,12 @@ struct Stepper : StepperBase {
       const int rows = (mode == 0 && Teff == 1 && cpb % 32 == 0) ? C->T : Teff;
       dim3 block(cpb, rows);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
-      if (visc) {
+      if (visc || C->gphi_sp) {
         ProfScope ps_(C, "k_interior");
-        launch<InteriorVisc<D, P>>(C, "k_interior", k_interior_visc<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops,
-                                   g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2],
-                                   C->trace[0], C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2], C->Gv[0],
-                                   C->Gv[1], C->Gv[2]);
+        launch<InteriorExt<D, P>>(C, "k_interior", k_interior_ext<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops,
+                                  g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2],
+                                  C->trace[0], C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2],
+                                  visc ? C->Gv[0] : nullptr, C->Gv[1], C->Gv[2], (const double*)C->gphi_sp);
       } else {
         ProfScope ps_(C, "k_interior");
         launch<Interior<D, P>>(C, "k_interior", k_interior<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops, g, mode,
@@ -248,7 +248,7 @@ struct Stepper : StepperBase {
         ProfScope ps_(C, "k_fv_candidate");
         launch<FvCandidate<D>>(C, "k_fv_candidate", k_fv_candidate<D>, blocks_for(g.Nq, BS), BS, 0, g, C->fvg, C->dt,
                                w_i, FH[0], FH[1], FH[2], C->U_cv, C->U_new, C->ext_old, C->ext_new,
-                               cf.FB ? (i == 0 ? 1 : 2) : 0);
+                               cf.FB ? (i == 0 ? 1 : 2) : 0, (const double*)C->gphi_fv);
       }
       CKL();
       if (cf.FB && C->tape_mode == 2) {
@@ -438,7 +438,8 @@ struct Stepper : StepperBase {
       ProfScope ps_(C, "k_fv_correct");
       launch<FvCorrect<D>>(C, "k_fv_correct", k_fv_correct<D>, (unsigned)nb, 128, 0, g, C->fvg, C->dt, w_i,
                            C->cfg.godunov, C->list_q, C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
-                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new, ext_new);
+                           C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new, ext_new,
+                           (const double*)C->gphi_fv);
     }
   }
 

@@ -137,3 +137,26 @@ def kelvin_helmholtz(N, seed=0, amp=0.01, noise=1e-3):
             return 2.5 * np.ones(x.shape)
         return np.ones(x.shape)
     return f
+
+
+def gravity_column(g=1.0, amp=1e-2, step=False):
+    """Isothermal atmosphere at rest in the gravity potential phi = g * x_last
+    (case -1 returns phi, as the reference's init_potential samples it,
+    src/sdader_simulator.py:425-434): P = exp(-g x_last) and rho = P (1 +
+    amp sin(2 pi x_0)) for ndim > 1 (with ``step``, the sign of the sine: a
+    density jump), so hydrostatic balance holds up to the perturbation."""
+    def f(xyz, case):
+        d = xyz.shape[0]
+        z = xyz[d - 1]
+        if case == -1:
+            return g * z
+        base = np.exp(-g * z)
+        if case == 0:
+            if d == 1:
+                return base
+            s = np.sin(2 * np.pi * xyz[0])
+            return base * (1.0 + amp * (np.sign(s) if step else s))
+        if 1 <= case <= d:
+            return np.zeros(z.shape)
+        return base
+    return f

@@ -148,6 +148,14 @@ class _DataManager:
         if name in ("U_sp", "U_cv", "W_cv") and sim._ctx is not None:
             sim._ctx.upload(name, np.asarray(value, dtype=np.float64))
             return
+        if name in ("grad_phi_sp", "grad_phi_fv") and sim._ctx is not None and sim.potential:
+            # the gravity gradients: at the solution points (SD layout) and
+            # their subcell averages (FV layout, sent in the SD layout)
+            value = np.ascontiguousarray(value, dtype=np.float64)
+            if name == "grad_phi_sp":
+                sim._ctx.upload("grad_phi_sp", value)
+            else:
+                sim._ctx.upload("grad_phi_cv", np.ascontiguousarray(sim.transpose_to_sd(value)))
         object.__getattribute__(self, "_host")[name] = value
 
 
@@ -319,14 +327,14 @@ class SD_Simulator(Simulator):
     GPU.  Constructed on its own it steps with the SD update and no
     limiter; SDADER_Simulator (its subclass) adds the options of the
     reference's SDADER class.  Options the GPU step does not implement
-    (potential, WB, isothermal, predictor=False, and viscosity with the FV
-    update and FB, which fails in the reference itself) raise
-    NotImplementedError here, before any device work.
+    (WB, isothermal, predictor=False, and viscosity with the FV update and
+    FB, which fails in the reference itself) raise NotImplementedError
+    here, before any device work.
     """
 
     def __init__(self, riemann_solver_sd: str = "llf", update: str = "SD", *args, **kwargs):
         super().__init__(*args, **kwargs)
-        for flag, name in ((self.isothermal, "isothermal"), (self.potential, "potential"), (self.WB, "WB")):
+        for flag, name in ((self.isothermal, "isothermal"), (self.WB, "WB")):
             if flag:
                 raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
         # options of the classes below SD_Simulator in the reference's chain
@@ -400,7 +408,25 @@ class SD_Simulator(Simulator):
         self._ctx.upload("U_cv", U_cv)
         self._ctx.upload("W_cv", W_cv)
         self._init_boundaries(U_sp, W_gh)
+        if self.potential:
+            self.init_potential()
         self.compute_dt()
+
+    def init_potential(self) -> None:
+        """Gradient of the gravity potential phi = init_fct(xyz, -1)
+        (src/sdader_simulator.py:425-434): cell means with one ghost element
+        layer, the solution-point values, their derivative inside each
+        element divided by h, cropped; and its subcell averages.  Host NumPy
+        at setup, as in the reference; uploaded to the device."""
+        phi_cv = quadrature_mean(self.mesh_cv, self.init_fct, self.ndim, -1)
+        phi_sp = self.compute_sp_from_cv(phi_cv[None])
+        grad = self.array_sp()[:self.ndim]
+        for dim in self.dims:
+            idim = self.dims[dim]
+            phi_fp = self.compute_fp_from_sp(phi_sp, dim)
+            grad[idim] = self.crop(self.compute_sp_from_dfp(phi_fp, dim)) / self.h[dim]
+        self.dm.grad_phi_sp = grad
+        self.dm.grad_phi_fv = self.transpose_to_fv(self.compute_cv_from_sp(grad))
 
 
     # ------------------------------------------------------------------
@@ -482,6 +508,7 @@ class SD_Simulator(Simulator):
         cfg.max_rho = self.max_rho
         cfg.min_P = self.min_P
         cfg.godunov = int(bool(self.godunov))
+        cfg.potential = int(bool(self.potential))
         cfg.viscosity = int(bool(self.viscosity))
         cfg.nu = float(self.nu)
         cfg.beta = float(self.beta)
@@ -734,7 +761,7 @@ class SD_Simulator(Simulator):
                     riemann_solver_fv=self.riemann_solver_fv_name, slope_limiter=self.slope_limiter_name,
                     BC=[list(self.BC[d]) for d in self.dims], gamma=self.gamma, cfl_coeff=self.cfl_coeff,
                     lims=[list(self.lim[d]) for d in self.dims], viscosity=bool(self.viscosity), nu=self.nu,
-                    beta=self.beta)
+                    beta=self.beta, potential=bool(self.potential))
 
     def save_state(self, path) -> None:
         """Write U_sp, U_cv, W_cv, the FV boundary buffers, time, n_step, dt

@@ -81,6 +81,21 @@ CASES = {
                                             ("sedov", {"N": 4}), 3),
     "visc_sod16_p3_sd_llf_eq": (dict(p=3, N=(16,), update="SD", riemann_solver_sd="llf", viscosity=True, nu=1e-3,
                                      BC=(("eq", "eq"),)), ("sod", {}), 5),
+    # gravity potential (src/sdader_simulator.py:425-434, src/simulator.py:197-203)
+    "pot_column8_p2_sd_hllc_reflective": (dict(p=2, N=(8, 8), update="SD", riemann_solver_sd="hllc", potential=True,
+                                               BC=(("periodic", "periodic"), ("reflective", "reflective"))),
+                                          ("gravity_column", {}), 5),
+    "pot_column8_p3_fvfb_hllc_gradfree": (dict(p=3, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                               riemann_solver_fv="hllc", potential=True,
+                                               BC=(("periodic", "periodic"), ("gradfree", "gradfree"))),
+                                          ("gravity_column", {"g": 2.0, "amp": 0.5, "step": True}), 4),
+    "pot_column4_p2_fv_llf_3d": (dict(p=2, N=(4, 3, 5), update="FV", riemann_solver_sd="llf", potential=True,
+                                      BC=(("periodic", "periodic"), ("periodic", "periodic"),
+                                          ("reflective", "reflective"))),
+                                 ("gravity_column", {"g": 1.5}), 3),
+    "pot_visc_column16_p3_sd_llf_1d": (dict(p=3, N=(16,), update="SD", riemann_solver_sd="llf", potential=True,
+                                            viscosity=True, nu=1e-3, BC=(("reflective", "reflective"),)),
+                                       ("gravity_column", {}), 4),
 }
 
 
@@ -125,7 +140,7 @@ def make_ic(spec):
     name, kw = spec
     if name == "vortex":
         return ics.isentropic_vortex()
-    if name in ("sedov", "kelvin_helmholtz"):
+    if name in ("sedov", "kelvin_helmholtz", "gravity_column"):
         return getattr(ics, name)(**kw)
     return getattr(ics, name)
 
@@ -169,6 +184,9 @@ def main(ref_root, only=None, long=False):
             out[f"init_BC_fp_{d}"] = getattr(s.dm, f"BC_fp_{d}").copy()
             if s.update == "FV":
                 out[f"init_BC_fv_{d}"] = getattr(s.dm, f"BC_fv_{d}").copy()
+        if s.potential:
+            out["grad_phi_sp"] = s.dm.grad_phi_sp.copy()
+            out["grad_phi_fv"] = s.dm.grad_phi_fv.copy()
         s.init_sim()
         dts = []
         for _ in range(steps):

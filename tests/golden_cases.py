@@ -50,7 +50,7 @@ def make_ic(spec):
     name, kw = spec
     if name == "vortex":
         return ics.isentropic_vortex()
-    if name in ("sedov", "kelvin_helmholtz"):
+    if name in ("sedov", "kelvin_helmholtz", "gravity_column"):
         return getattr(ics, name)(**kw)
     return getattr(ics, name)
 
@@ -67,6 +67,9 @@ def oracle_from_golden(data, kw):
     U_cv = data["init_U_cv"] if "init_U_cv" in data else compute_conservatives(data["init_W_cv"], ndim,
                                                                                  kw.get("gamma", 1.4))
     state = {"U_sp": data["init_U_sp"], "U_cv": U_cv, "W_cv": data["init_W_cv"]}
+    if kw.get("potential", False):
+        state["grad_phi_sp"] = data["grad_phi_sp"]
+        state["grad_phi_fv"] = data["grad_phi_fv"]
     for d in DIMS[:ndim]:
         state[f"BC_fp_{d}"] = data[f"init_BC_fp_{d}"]
         if f"init_BC_fv_{d}" in data:
@@ -80,7 +83,7 @@ def oracle_from_golden(data, kw):
         PAD=kw.get("PAD", True), blending=kw.get("blending", True), min_rho=kw.get("min_rho", 1e-10),
         max_rho=kw.get("max_rho", 1e10), min_P=kw.get("min_P", 1e-10), godunov=kw.get("godunov", False),
         ops=ops, state=state, viscosity=kw.get("viscosity", False), nu=kw.get("nu", 1e-4),
-        beta=kw.get("beta", 2.0 / 3))
+        beta=kw.get("beta", 2.0 / 3), potential=kw.get("potential", False))
 
 
 def golden_operators(data):

@@ -16,6 +16,9 @@ def product_from_golden(data, kw, meta):
     # before recomputing it from U_sp (FV) or at the end of a run (SD)
     s.dm.U_cv = data["init_U_cv"] if "init_U_cv" in data else s.compute_conservatives(data["init_W_cv"])
     s.dm.W_cv = data["init_W_cv"]
+    if kw.get("potential", False):
+        s.dm.grad_phi_sp = data["grad_phi_sp"]
+        s.dm.grad_phi_fv = data["grad_phi_fv"]
     return s
 
 
@@ -46,7 +49,11 @@ def oracle_like(s, **override):
               riemann_solver_sd=s.riemann_solver_sd_name, riemann_solver_fv=s.riemann_solver_fv_name,
               slope_limiter=s.slope_limiter_name, update=s.update, FB=s.FB, tolerance=s.tolerance, SED=s.SED,
               NAD=s.NAD, PAD=s.PAD, blending=s.blending, min_rho=s.min_rho, max_rho=s.max_rho, min_P=s.min_P,
-              godunov=s.godunov, ops=s.ops, state=state)
+              godunov=s.godunov, ops=s.ops, state=state, viscosity=s.viscosity, nu=s.nu, beta=s.beta,
+              potential=s.potential)
+    if s.potential:
+        state["grad_phi_sp"] = s.dm.grad_phi_sp
+        state["grad_phi_fv"] = s.dm.grad_phi_fv
     kw.update(override)
     return OracleSDADER(**kw)
 

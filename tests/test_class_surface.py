@@ -76,3 +76,33 @@ def test_integrate_faces_averages_the_other_directions():
     out = s.integrate_faces(M, "x")
     assert out.shape == M.shape
     assert np.allclose(out, 2.5, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["pot_column8_p2_sd_hllc_reflective", "pot_column4_p2_fv_llf_3d",
+                                  "pot_visc_column16_p3_sd_llf_1d"])
+def test_potential_gradients_match_reference(name):
+    """init_potential (src/sdader_simulator.py:425-434) on the host: the
+    gradient at the solution points and its subcell averages equal the
+    reference's, bit for bit (x86_64, where the fixtures were made)."""
+    import platform
+    from golden_cases import load, make_ic
+    from spd_gb300.simulator import mesh_cv
+    data, kw, meta = load(name)
+    s = object.__new__(SDADER_Simulator)
+    Simulator.__init__(s, p=kw["p"], N=kw["N"], init_fct=make_ic(meta["ic"]),
+                       **{k: kw[k] for k in ("xlim", "ylim", "zlim") if k in kw})
+    s.ops = SDADER_Simulator.build_operators(kw["p"], kw["p"])
+    s.n = {d: kw["p"] + 1 for d in s.dims}
+    s.nader = kw["p"] + 1
+    s.fp = {d: s.ops["x_fp"] for d in s.dims}
+    s.mesh_cv = mesh_cv(s.ndim, [s.N[d] for d in s.dims], s.p, [s.lim[d] for d in s.dims], s.Nghe, s.ops["x_fp"])
+    s.potential = True
+    s.init_potential()
+    same = platform.machine() in ("x86_64", "AMD64")
+    for key in ("grad_phi_sp", "grad_phi_fv"):
+        got, want = getattr(s.dm, key), data[key]
+        assert got.shape == want.shape
+        if same:
+            assert np.array_equal(got, want), key
+        else:
+            assert np.allclose(got, want, rtol=1e-13, atol=1e-13), key

@@ -224,7 +224,7 @@ def test_viscosity_vs_oracle(name):
     kw["init_fct"] = {"four_quadrant": ics.four_quadrant, "sod": ics.sod, "sedov4": ics.sedov(4)}[init]
     from spd_gb300 import SDADER_Simulator
     s = SDADER_Simulator(verbose=False, **kw)
-    o = oracle_like(s, viscosity=True, nu=kw["nu"], beta=kw.get("beta", 2.0 / 3))
+    o = oracle_like(s)
     dts = step_both(s, o, 3)
     assert all(a == b for a, b in dts), dts
     assert not compare(s, o)
