@@ -124,6 +124,8 @@ typedef struct spd_config {
   /* gravity potential source terms (src/simulator.py:197-203) in the
    * predictor's dUdt and the subcell update; gradients by spd_upload */
   int potential;
+  /* isothermal system (src/hydro.py:84,123,169, src/riemann_solver.py:142,210) */
+  int isothermal;
 } spd_config;
 
 /* Constant operators built at setup on the host

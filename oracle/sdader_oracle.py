@@ -267,8 +267,9 @@ def axis_order(idim):
 # ----------------------------------------------------------------------------
 # hydro (src/hydro.py)
 # ----------------------------------------------------------------------------
-def compute_primitives(U, ndim, gamma, vels=None):
-    """src/hydro.py:48-86 (U -> W); the kinetic term sums in ``vels`` order."""
+def compute_primitives(U, ndim, gamma, vels=None, iso=False):
+    """src/hydro.py:48-86 (U -> W); the kinetic term sums in ``vels`` order;
+    ``iso``: the isothermal system multiplies the kinetic term by 0."""
     _p_ = ndim + 1
     comp = {0: U[0]}
     K = None
@@ -276,11 +277,13 @@ def compute_primitives(U, ndim, gamma, vels=None):
         comp[vel] = U[vel] / U[0]
         K = comp[vel] * comp[vel] if K is None else K + comp[vel] * comp[vel]
     K = K * (0.5 * U[0])
+    if iso:
+        K = K * 0
     comp[_p_] = (gamma - 1) * (U[_p_] - K)
     return xp.stack([comp[v] for v in range(ndim + 2)], 0)
 
 
-def compute_conservatives(W, ndim, gamma, vels=None):
+def compute_conservatives(W, ndim, gamma, vels=None, iso=False):
     """src/hydro.py:88-125 (W -> U); the kinetic term sums in ``vels`` order."""
     _p_ = ndim + 1
     comp = {0: W[0]}
@@ -289,12 +292,15 @@ def compute_conservatives(W, ndim, gamma, vels=None):
         comp[vel] = W[vel] * W[0]
         K = W[vel] * W[vel] if K is None else K + W[vel] * W[vel]
     K = K * (0.5 * W[0])
+    if iso:
+        K = K * 0
     comp[_p_] = W[_p_] / (gamma - 1) + K
     return xp.stack([comp[v] for v in range(ndim + 2)], 0)
 
 
-def compute_fluxes(W, vels, gamma):
-    """src/hydro.py:127-170; ``vels`` is the rotated velocity index list."""
+def compute_fluxes(W, vels, gamma, iso=False):
+    """src/hydro.py:127-170; ``vels`` is the rotated velocity index list;
+    the isothermal system multiplies the energy flux by 0."""
     ndim = len(vels)
     _p_ = ndim + 1
     comp = {}
@@ -309,6 +315,8 @@ def compute_fluxes(W, vels, gamma):
     comp[0] = m
     comp[v1] = m * W[v1] + W[_p_]
     comp[_p_] = W[v1] * (E + W[_p_])
+    if iso:
+        comp[_p_] = comp[_p_] * 0
     return xp.stack([comp[v] for v in range(ndim + 2)], 0)
 
 
@@ -341,37 +349,37 @@ def compute_cs(P, rho, gamma, min_c2):
 # ----------------------------------------------------------------------------
 # Riemann solvers (src/riemann_solver.py)
 # ----------------------------------------------------------------------------
-def riemann(name, M_L, M_R, vels, gamma, min_c2, prims):
+def riemann(name, M_L, M_R, vels, gamma, min_c2, prims, iso=False):
     """src/riemann_solver.py:10-29 wrapper, then llf/hllc/lhllc."""
     ndim = len(vels)
     if prims:
         W_L, W_R = M_L, M_R
-        U_L = compute_conservatives(W_L, ndim, gamma, vels)
-        U_R = compute_conservatives(W_R, ndim, gamma, vels)
+        U_L = compute_conservatives(W_L, ndim, gamma, vels, iso)
+        U_R = compute_conservatives(W_R, ndim, gamma, vels, iso)
     else:
         U_L, U_R = M_L, M_R
-        W_L = compute_primitives(U_L, ndim, gamma, vels)
-        W_R = compute_primitives(U_R, ndim, gamma, vels)
+        W_L = compute_primitives(U_L, ndim, gamma, vels, iso)
+        W_R = compute_primitives(U_R, ndim, gamma, vels, iso)
     if name == "llf":
-        return _llf(W_L, W_R, U_L, U_R, vels, gamma, min_c2)
+        return _llf(W_L, W_R, U_L, U_R, vels, gamma, min_c2, iso)
     if name in ("hllc", "lhllc"):
-        return _hllc(W_L, W_R, U_L, U_R, vels, gamma, min_c2, low_mach=(name == "lhllc"))
+        return _hllc(W_L, W_R, U_L, U_R, vels, gamma, min_c2, low_mach=(name == "lhllc"), iso=iso)
     raise AttributeError(name)
 
 
-def _llf(W_L, W_R, U_L, U_R, vels, gamma, min_c2):
+def _llf(W_L, W_R, U_L, U_R, vels, gamma, min_c2, iso=False):
     """src/riemann_solver.py:31-65."""
     _p_ = len(vels) + 1
     v1 = vels[0]
-    F_L = compute_fluxes(W_L, vels, gamma)
-    F_R = compute_fluxes(W_R, vels, gamma)
+    F_L = compute_fluxes(W_L, vels, gamma, iso)
+    F_R = compute_fluxes(W_R, vels, gamma, iso)
     c_L = compute_cs(W_L[_p_], W_L[0], gamma, min_c2) + xp.abs(W_L[v1])
     c_R = compute_cs(W_R[_p_], W_R[0], gamma, min_c2) + xp.abs(W_R[v1])
     c_max = xp.where(c_L > c_R, c_L, c_R)[None, ...]
     return 0.5 * (F_R + F_L) - 0.5 * c_max * (U_R - U_L)
 
 
-def _hllc(W_L, W_R, U_L, U_R, vels, gamma, min_c2, low_mach=False):
+def _hllc(W_L, W_R, U_L, U_R, vels, gamma, min_c2, low_mach=False, iso=False):
     """src/riemann_solver.py:67-145 (hllc) and :147-212 (lhllc)."""
     _p_ = len(vels) + 1
     v1 = vels[0]
@@ -405,6 +413,8 @@ def _hllc(W_L, W_R, U_L, U_R, vels, gamma, min_c2, low_mach=False):
     comp[_p_] = v_gdv * (e_gdv + P_gdv)
     for vel in vels[1:]:
         comp[vel] = comp[0] * xp.where(v_star > 0, W_L[vel], W_R[vel])
+    if iso:
+        comp[_p_] = comp[_p_] * 0
     return xp.stack([comp[v] for v in range(len(vels) + 2)], 0)
 
 
@@ -502,7 +512,8 @@ class OracleSDADER:
     def __init__(self, *, ndim, N, p, m, lims, BC, gamma, cfl_coeff, min_c2,
                  riemann_solver_sd, riemann_solver_fv, slope_limiter, update,
                  FB, tolerance, SED, NAD, PAD, blending, min_rho, max_rho,
-                 min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3, potential=False):
+                 min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3, potential=False,
+                 isothermal=False):
         self.ndim = ndim
         self.N = list(N)          # cells per dim, x first
         self.p = p
@@ -533,6 +544,7 @@ class OracleSDADER:
         self.nu = nu
         self.beta = beta
         self.potential = potential
+        self.iso = isothermal
         self.ngh = Nghc
         self.ops = {k: (_Mat(v) if k in ("sp_to_fp", "dfp_to_sp", "sp_to_cv", "cv_to_sp", "invader", "w_tp")
                         else v) for k, v in ops.items()}
@@ -631,9 +643,9 @@ class OracleSDADER:
             M_fp = apply_axis(ops["sp_to_fp"], U_ader, ax_sp, axis_order(idim))
             # interior flux points (the edge values are replaced below)
             M_in = _shift(M_fp, 1, -1, ax_sp)
-            F_in = compute_fluxes(compute_primitives(M_in, nd, self.gamma), vels, self.gamma)
+            F_in = compute_fluxes(compute_primitives(M_in, nd, self.gamma, iso=self.iso), vels, self.gamma, self.iso)
             ML, MR = self._interfaces(M_fp, idim)
-            F = riemann(self.rs_sd, ML, MR, vels, self.gamma, self.min_c2, prims=False)
+            F = riemann(self.rs_sd, ML, MR, vels, self.gamma, self.min_c2, prims=False, iso=self.iso)
             F_all[idim] = xp.cat([xp.expand(_shift(F, None, -1, ax_cell + 1), ax_sp), F_in,
                                   xp.expand(_shift(F, 1, None, ax_cell + 1), ax_sp)], ax_sp)
             M_all[idim] = M_fp
@@ -699,7 +711,7 @@ class OracleSDADER:
         nd = self.ndim
         W_fp, dW_sp = {}, {}
         for idim in range(nd):
-            Wf = compute_primitives(M_all[idim], nd, self.gamma)
+            Wf = compute_primitives(M_all[idim], nd, self.gamma, iso=self.iso)
             ML, _ = self._interfaces(Wf, idim)
             W_fp[idim] = self._apply_interfaces(ML, Wf, idim)
             dW_sp[idim] = apply_axis(self.ops["dfp_to_sp"], W_fp[idim], sp_axis(nd, idim),
@@ -735,7 +747,8 @@ class OracleSDADER:
         for idim in range(self.ndim):
             vel = idim + 1
             comp[vel] = comp[vel] + U[0] * grad_phi[idim]
-            comp[_p_] = comp[_p_] + U[vel] * grad_phi[idim]
+            if not self.iso:
+                comp[_p_] = comp[_p_] + U[vel] * grad_phi[idim]
         return xp.stack(comp, 0)
 
     def ader_predictor(self):
@@ -896,8 +909,8 @@ class OracleSDADER:
         nd = self.ndim
         U_cv = xp.detach(U_cv)
         U_new = xp.detach(U_new)
-        W_old = compute_primitives(U_cv, nd, self.gamma)
-        W_new = compute_primitives(U_new, nd, self.gamma)
+        W_old = compute_primitives(U_cv, nd, self.gamma, iso=self.iso)
+        W_new = compute_primitives(U_new, nd, self.gamma, iso=self.iso)
         M = self.fv_boundaries(self.pad(W_old))
         act = (slice(None),) + (slice(g, -g),) * nd
         center = M[act]
@@ -1062,7 +1075,7 @@ class OracleSDADER:
             crop_s[ax] = slice(None, -1)
             ML = pred[tuple(crop_m)] + S[idim][tuple(crop_s)]
             F[idim] = riemann(self.rs_fv, ML, MR, self.rolled_vels(idim), self.gamma,
-                              self.min_c2, prims=True)
+                              self.min_c2, prims=True, iso=self.iso)
         return F
 
     def _embed(self, M, inner):
@@ -1086,7 +1099,7 @@ class OracleSDADER:
         Ffaces = self.integrate_faces(F_all)
         w = self.ops["w_tp"]
         for i in range(self.T):
-            W_cv = compute_primitives(U_cv, nd, self.gamma)
+            W_cv = compute_primitives(U_cv, nd, self.gamma, iso=self.iso)
             dt = self.dt * w[i]
             F_HO = self.store_high_order_fluxes(Ffaces, i)
             U_new = self.fv_apply_fluxes(U_cv, F_HO, dt)
@@ -1117,12 +1130,12 @@ class OracleSDADER:
             self.ader_update(F_all)
         else:
             self.fv_update(F_all)
-        self.W_cv = compute_primitives(self.U_cv, self.ndim, self.gamma)
+        self.W_cv = compute_primitives(self.U_cv, self.ndim, self.gamma, iso=self.iso)
         self.time += self.dt
 
     def end_sim(self):
         self.U_cv = apply_full(self.ops["sp_to_cv"], self.U_sp, self.ndim)
-        self.W_cv = compute_primitives(self.U_cv, self.ndim, self.gamma)
+        self.W_cv = compute_primitives(self.U_cv, self.ndim, self.gamma, iso=self.iso)
 
     def perform_iterations(self, n_step):
         for _ in range(n_step):

@@ -74,6 +74,7 @@ class spd_config(ctypes.Structure):
         ("nu", ctypes.c_double),
         ("beta", ctypes.c_double),
         ("potential", ctypes.c_int),
+        ("isothermal", ctypes.c_int),
     ]
 
 

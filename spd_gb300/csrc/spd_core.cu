@@ -183,6 +183,7 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
   }
   g.gamma = cfg->gamma;
   g.min_c2 = cfg->min_c2;
+  g.iso = cfg->isothermal ? 1 : 0;
   C->h_dt = h_min / (double)(P + 1);
   // viscous dt limit h**2/nu*.25 (src/sd_simulator.py:223-224); h*h is the
   // correctly rounded square, as Python's h**2

@@ -279,8 +279,10 @@ SPD_FN int rvel(int idim, int k) { return 1 + (idim + k) % D; }
 // velocity list, which is the rotated list inside the Riemann wrapper
 // (src/riemann_solver.py:10-29) and the plain list elsewhere.
 // ``r0_out`` (optional) receives 1/rho for later quotients by rho.
+// ``iso``: the isothermal system (src/hydro.py:84,123,169): the kinetic term
+// of the energy is multiplied by 0 and the energy flux by 0.
 template <int D, class S>
-SPD_FN void prim(const S* U, S* W, double gamma, int idim_order, S* r0_out = nullptr) {
+SPD_FN void prim(const S* U, S* W, double gamma, int idim_order, S* r0_out = nullptr, bool iso = false) {
   constexpr int P_ = D + 1;
   W[0] = U[0];
   S K = 0.0;
@@ -294,12 +296,13 @@ SPD_FN void prim(const S* U, S* W, double gamma, int idim_order, S* r0_out = nul
     K = (k == 0) ? w2 : K + w2;
   }
   K = K * (0.5 * U[0]);
+  if (iso) K = K * 0.0;
   W[P_] = (gamma - 1.0) * (U[P_] - K);
 }
 
 // W -> U (src/hydro.py:88-125).
 template <int D, class S>
-SPD_FN void cons(const S* W, S* U, double gamma, int idim_order) {
+SPD_FN void cons(const S* W, S* U, double gamma, int idim_order, bool iso = false) {
   constexpr int P_ = D + 1;
   U[0] = W[0];
   S K = 0.0;
@@ -311,12 +314,13 @@ SPD_FN void cons(const S* W, S* U, double gamma, int idim_order) {
     K = (k == 0) ? w2 : K + w2;
   }
   K = K * (0.5 * W[0]);
+  if (iso) K = K * 0.0;
   U[P_] = div_by(W[P_], gamma - 1.0, 1.0 / (gamma - 1.0)) + K;
 }
 
 // Euler flux in the rotated frame of direction idim (src/hydro.py:127-170).
 template <int D, class S>
-SPD_FN void flux(const S* W, S* F, double gamma, int idim) {
+SPD_FN void flux(const S* W, S* F, double gamma, int idim, bool iso = false) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
   S K = 0.0, m = 0.0;
@@ -332,6 +336,7 @@ SPD_FN void flux(const S* W, S* F, double gamma, int idim) {
   F[0] = m;
   F[v1] = m * W[v1] + W[P_];
   F[P_] = W[v1] * (E + W[P_]);
+  if (iso) F[P_] = F[P_] * 0.0;
 }
 
 // Sound speed with floor (src/hydro.py:3-46).
@@ -347,12 +352,12 @@ SPD_FN S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
 template <int D, class S, int BM = 0>
 SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
                                     double min_c2, int idim, Br<BM>* br = nullptr, const S* rL = nullptr,
-                                    const S* rR = nullptr) {
+                                    const S* rR = nullptr, bool iso = false) {
   constexpr int V = D + 2, P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
   S FL[V], FR[V];
-  flux<D>(WL, FL, gamma, idim);
-  flux<D>(WR, FR, gamma, idim);
+  flux<D>(WL, FL, gamma, idim, iso);
+  flux<D>(WR, FR, gamma, idim, iso);
   const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
   const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br, rR) + abs_br(WR[v1], br);
   const S cmax = pick(br, cL > cR) ? cL : cR;
@@ -366,7 +371,7 @@ SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double
 template <int D, class S, int BM = 0>
 SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double gamma,
                                      double min_c2, int idim, bool low_mach, Br<BM>* br = nullptr,
-                                     const S* rL = nullptr, const S* rR = nullptr) {
+                                     const S* rL = nullptr, const S* rR = nullptr, bool iso = false) {
   constexpr int P_ = D + 1;
   const int v1 = rvel<D>(idim, 0);
   const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
@@ -444,13 +449,14 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
       F[v] = F[0] * (left ? WL[v] : WR[v]);
     }
   }
+  if (iso) F[P_] = F[P_] * 0.0;
 }
 
 // Riemann wrapper (src/riemann_solver.py:10-29): inputs conservative
 // (prims=false) or primitive (prims=true); rotated velocity order.
 template <int D, class S, int BM = 0>
 SPD_FN void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, double min_c2,
-                                        int idim, bool prims, Br<BM>* br = nullptr) {
+                                        int idim, bool prims, Br<BM>* br = nullptr, bool iso = false) {
   constexpr int V = D + 2;
   S WL[V], WR[V], UL[V], UR[V];
   S rL, rR;  // 1/rho of the two states when the conversion computed it
@@ -459,18 +465,18 @@ SPD_FN void riemann(int solver, const S* ML, const S* MR, S* F, double gamma, do
   if (prims) {
 #pragma unroll
     for (int v = 0; v < V; ++v) { WL[v] = ML[v]; WR[v] = MR[v]; }
-    cons<D>(WL, UL, gamma, idim);
-    cons<D>(WR, UR, gamma, idim);
+    cons<D>(WL, UL, gamma, idim, iso);
+    cons<D>(WR, UR, gamma, idim, iso);
   } else {
 #pragma unroll
     for (int v = 0; v < V; ++v) { UL[v] = ML[v]; UR[v] = MR[v]; }
-    prim<D>(UL, WL, gamma, idim, &rL);
-    prim<D>(UR, WR, gamma, idim, &rR);
+    prim<D>(UL, WL, gamma, idim, &rL, iso);
+    prim<D>(UR, WR, gamma, idim, &rR, iso);
     prL = &rL;
     prR = &rR;
   }
-  if (solver == RS_LLF) llf<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, br, prL, prR);
-  else hllc<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC, br, prL, prR);
+  if (solver == RS_LLF) llf<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, br, prL, prR, iso);
+  else hllc<D, S, BM>(WL, WR, UL, UR, F, gamma, min_c2, idim, solver == RS_LHLLC, br, prL, prR, iso);
 }
 
 // One output of a 1D operator contraction: sum_s A[s] * x[s].  ``lanes2``

@@ -85,7 +85,7 @@ __device__ __forceinline__ void potential_source(const Geo& g, const double* __r
   for (int d = 0; d < D; ++d) {
     const double gp = gphi[(long long)d * g.Nq + q];
     dudt[d + 1] = dudt[d + 1] + u[0] * gp;
-    dudt[D + 1] = dudt[D + 1] + u[d + 1] * gp;
+    if (!g.iso) dudt[D + 1] = dudt[D + 1] + u[d + 1] * gp;
   }
 }
 
@@ -147,11 +147,11 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
 #pragma unroll
       for (int v = 0; v < V; ++v) W[v] = ext_new[(long long)v * g.Nqe + e];
     } else {
-      prim<D>(u, W, g.gamma, 0);
+      prim<D>(u, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_old[(long long)v * g.Nqe + e] = W[v];
-    prim<D>(un, W, g.gamma, 0);
+    prim<D>(un, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
   }
@@ -776,7 +776,7 @@ static __device__ __forceinline__ void face(const Geo& g, int d, int solver, lon
   }
   Br<BM> br;
   if (BM == 2) br.w = ftape[fidx];
-  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, true, &br);
+  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, true, &br, g.iso != 0);
   if (BM == 1) ftape[fidx] = br.w;
 #pragma unroll
   for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = F[v];
@@ -847,7 +847,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
     // (k_fv_candidate with write_ext == 2) or, after the last substep, W_cv
     // (k_ext_to_plain)
     double W[V];
-    prim<D>(un, W, g.gamma, 0);
+    prim<D>(un, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
     const long long e = ext_of<D>(g, ix, iy, iz);
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];

@@ -41,6 +41,7 @@ struct Geo {
   int h_pow2[3];
   double gamma, min_c2;
   int bc[3][2];
+  int iso;  // isothermal (src/hydro.py:84,123,169)
 };
 
 template <int D, int P>
@@ -227,7 +228,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   double F[k::V];
   Br<BM> br;
   if (BM == 2) br.w = tape[tid];
-  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, false, &br);
+  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, false, &br, g.iso != 0);
   if (BM == 1) tape[tid] = br.w;
 #pragma unroll
   for (int v = 0; v < k::V; ++v) Fi[(((long long)v * g.T + t) * k::NJ + j) * nI + iface] = F[v];
@@ -300,8 +301,8 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
           double M[k::V], W[k::V], F[k::V];
 #pragma unroll
           for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
-          prim<D>(M, W, g.gamma, 0);
-          flux<D>(W, F, g.gamma, d);
+          prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+          flux<D>(W, F, g.gamma, d, g.iso != 0);
 #pragma unroll
           for (int v = 0; v < k::V; ++v) Fl[v][f] = F[v];
         }
@@ -351,8 +352,10 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
           const double uv = Uin[(((long long)(d + 1) * Tu + tu) * k::NS + s) * g.Nc + c];
           double* sv = &dudt_s[((((long long)(d + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
           *sv = *sv + u0 * gp;
-          double* sp = &dudt_s[((((long long)(D + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
-          *sp = *sp + uv * gp;
+          if (!g.iso) {
+            double* sp = &dudt_s[((((long long)(D + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
+            *sp = *sp + uv * gp;
+          }
         }
       }
     }

@@ -51,7 +51,7 @@ struct PrimOnly {
     double u[V], W[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) u[v] = U_cv[(long long)v * g.Nq + q];
-    prim<D>(u, W, g.gamma, 0);
+    prim<D>(u, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
 #pragma unroll
     for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
   }

@@ -74,7 +74,7 @@ struct ViscGrad {
           double M[k::V], W[k::V];
 #pragma unroll
           for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
-          prim<D>(M, W, g.gamma, 0);
+          prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
 #pragma unroll
           for (int v = 0; v < k::V; ++v) Wf[v][f] = W[v];
         }
@@ -88,7 +88,7 @@ struct ViscGrad {
           } else {
 #pragma unroll
             for (int v = 0; v < k::V; ++v) M[v] = tr(1, v, c);
-            prim<D>(M, W, g.gamma, 0);
+            prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
           }
 #pragma unroll
           for (int v = 0; v < k::V; ++v) Wf[v][k::nf - 1] = W[v];
@@ -102,7 +102,7 @@ struct ViscGrad {
             const int side = (cd > 0 || b0 == BC_PERIODIC) ? 1 : 0;
 #pragma unroll
             for (int v = 0; v < k::V; ++v) M[v] = tr(side, v, src);
-            prim<D>(M, W, g.gamma, 0);
+            prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
             if (cd == 0 && b0 == BC_REFLECTIVE) W[d + 1] = W[d + 1] * -1.0;
           } else {
 #pragma unroll

@@ -30,7 +30,7 @@ from .polynomials import (ader_matrix, flux_points, gauss_legendre_quadrature, i
 DIMS = ("x", "y", "z")
 
 
-def _primitives(U, vels, _p_, gamma):
+def _primitives(U, vels, _p_, gamma, isothermal=False):
     """src/hydro.py:48-86 on the host (user-facing helper)."""
     W = U.copy()
     K = W[0].copy() * 0
@@ -38,11 +38,12 @@ def _primitives(U, vels, _p_, gamma):
         W[vel] = U[vel] / U[0]
         K += W[vel] ** 2
     K *= 0.5 * U[0]
+    K *= 0 if isothermal else 1
     W[_p_] = (gamma - 1) * (U[_p_] - K)
     return W
 
 
-def _conservatives(W, vels, _p_, gamma):
+def _conservatives(W, vels, _p_, gamma, isothermal=False):
     """src/hydro.py:88-125 on the host (setup and user-facing helper)."""
     U = W.copy()
     K = W[0].copy() * 0
@@ -50,6 +51,7 @@ def _conservatives(W, vels, _p_, gamma):
         U[vel] = W[vel] * U[0]
         K += W[vel] ** 2
     K *= 0.5 * U[0]
+    K *= 0 if isothermal else 1
     U[_p_] = W[_p_] / (gamma - 1) + K
     return U
 
@@ -81,7 +83,7 @@ def subcell_faces(N, h, fp_ref, ngh) -> np.ndarray:
     return fp
 
 
-def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1):
+def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1, isothermal=False):
     """Initial subcell averages of the primitives and the derived
     solution-point / conservative arrays (src/sd_simulator.py:74-90).
     Returns (W_gh, W_init_cv, W_sp, U_sp, U_cv)."""
@@ -100,8 +102,8 @@ def initial_state(ndim, N, p, lims, init_fct, ops, gamma, Nghe=1):
     W_init_cv = W_gh[(slice(None),) + (slice(Nghe, -Nghe),) * ndim + (Ellipsis,)]
     W_cv = W_init_cv.copy()
     W_sp = transform_full_threaded(W_cv, ops["cv_to_sp"], ndim)
-    U_sp = _conservatives(W_sp, vels, ndim + 1, gamma)
-    U_cv = _conservatives(W_cv, vels, ndim + 1, gamma)
+    U_sp = _conservatives(W_sp, vels, ndim + 1, gamma, isothermal)
+    U_cv = _conservatives(W_cv, vels, ndim + 1, gamma, isothermal)
     return W_gh, W_init_cv, W_sp, U_sp, U_cv
 
 
@@ -274,10 +276,10 @@ class Simulator:
         return M[(slice(None),) + (slice(ngh, -ngh),) * self.ndim + (Ellipsis,)]
 
     def compute_primitives(self, U, **kwargs) -> np.ndarray:
-        return _primitives(U, self.vels, self._p_, self.gamma)
+        return _primitives(U, self.vels, self._p_, self.gamma, self.isothermal)
 
     def compute_conservatives(self, W, **kwargs) -> np.ndarray:
-        return _conservatives(W, self.vels, self._p_, self.gamma)
+        return _conservatives(W, self.vels, self._p_, self.gamma, self.isothermal)
 
     def compute_positions(self):
         pass
@@ -327,14 +329,14 @@ class SD_Simulator(Simulator):
     GPU.  Constructed on its own it steps with the SD update and no
     limiter; SDADER_Simulator (its subclass) adds the options of the
     reference's SDADER class.  Options the GPU step does not implement
-    (WB, isothermal, predictor=False, and viscosity with the FV update and
-    FB, which fails in the reference itself) raise NotImplementedError
-    here, before any device work.
+    (WB, predictor=False, and viscosity with the FV update and FB, which
+    fails in the reference itself) raise NotImplementedError here, before
+    any device work.
     """
 
     def __init__(self, riemann_solver_sd: str = "llf", update: str = "SD", *args, **kwargs):
         super().__init__(*args, **kwargs)
-        for flag, name in ((self.isothermal, "isothermal"), (self.WB, "WB")):
+        for flag, name in ((self.WB, "WB"),):
             if flag:
                 raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
         # options of the classes below SD_Simulator in the reference's chain
@@ -399,7 +401,7 @@ class SD_Simulator(Simulator):
         self.compute_positions()
         W_gh, self.W_init_cv, W_sp, U_sp, U_cv = initial_state(
             ndim, [self.N[d] for d in self.dims], p, [self.lim[d] for d in self.dims], self.init_fct,
-            operators, self.gamma, self.Nghe)
+            operators, self.gamma, self.Nghe, self.isothermal)
         W_cv = self.W_init_cv.copy()
         self.dm.W_sp = W_sp
         # ---- device context ----------------------------------------------
@@ -509,6 +511,7 @@ class SD_Simulator(Simulator):
         cfg.min_P = self.min_P
         cfg.godunov = int(bool(self.godunov))
         cfg.potential = int(bool(self.potential))
+        cfg.isothermal = int(bool(self.isothermal))
         cfg.viscosity = int(bool(self.viscosity))
         cfg.nu = float(self.nu)
         cfg.beta = float(self.beta)
@@ -761,7 +764,7 @@ class SD_Simulator(Simulator):
                     riemann_solver_fv=self.riemann_solver_fv_name, slope_limiter=self.slope_limiter_name,
                     BC=[list(self.BC[d]) for d in self.dims], gamma=self.gamma, cfl_coeff=self.cfl_coeff,
                     lims=[list(self.lim[d]) for d in self.dims], viscosity=bool(self.viscosity), nu=self.nu,
-                    beta=self.beta, potential=bool(self.potential))
+                    beta=self.beta, potential=bool(self.potential), isothermal=bool(self.isothermal))
 
     def save_state(self, path) -> None:
         """Write U_sp, U_cv, W_cv, the FV boundary buffers, time, n_step, dt

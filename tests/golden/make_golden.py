@@ -96,6 +96,17 @@ CASES = {
     "pot_visc_column16_p3_sd_llf_1d": (dict(p=3, N=(16,), update="SD", riemann_solver_sd="llf", potential=True,
                                             viscosity=True, nu=1e-3, BC=(("reflective", "reflective"),)),
                                        ("gravity_column", {}), 4),
+    # isothermal system (src/hydro.py:84,123,169, src/riemann_solver.py:142,210)
+    "iso_quadrant8_p2_fvfb_hllc_gradfree": (dict(p=2, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                                 riemann_solver_fv="hllc", isothermal=True,
+                                                 BC=(("gradfree", "gradfree"),) * 2),
+                                            ("four_quadrant", {}), 4),
+    "iso_sod16_p3_sd_llf_reflective": (dict(p=3, N=(16,), update="SD", riemann_solver_sd="llf", isothermal=True,
+                                            BC=(("reflective", "reflective"),)), ("sod", {}), 5),
+    "iso_pot_column8_p2_fv_lhllc": (dict(p=2, N=(8, 8), update="FV", FB=True, riemann_solver_sd="lhllc",
+                                         riemann_solver_fv="llf", isothermal=True, potential=True,
+                                         BC=(("periodic", "periodic"), ("reflective", "reflective"))),
+                                    ("gravity_column", {"amp": 0.3, "step": True}), 3),
 }
 
 

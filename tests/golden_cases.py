@@ -83,7 +83,8 @@ def oracle_from_golden(data, kw):
         PAD=kw.get("PAD", True), blending=kw.get("blending", True), min_rho=kw.get("min_rho", 1e-10),
         max_rho=kw.get("max_rho", 1e10), min_P=kw.get("min_P", 1e-10), godunov=kw.get("godunov", False),
         ops=ops, state=state, viscosity=kw.get("viscosity", False), nu=kw.get("nu", 1e-4),
-        beta=kw.get("beta", 2.0 / 3), potential=kw.get("potential", False))
+        beta=kw.get("beta", 2.0 / 3), potential=kw.get("potential", False),
+        isothermal=kw.get("isothermal", False))
 
 
 def golden_operators(data):

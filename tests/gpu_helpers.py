@@ -50,7 +50,7 @@ def oracle_like(s, **override):
               slope_limiter=s.slope_limiter_name, update=s.update, FB=s.FB, tolerance=s.tolerance, SED=s.SED,
               NAD=s.NAD, PAD=s.PAD, blending=s.blending, min_rho=s.min_rho, max_rho=s.max_rho, min_P=s.min_P,
               godunov=s.godunov, ops=s.ops, state=state, viscosity=s.viscosity, nu=s.nu, beta=s.beta,
-              potential=s.potential)
+              potential=s.potential, isothermal=s.isothermal)
     if s.potential:
         state["grad_phi_sp"] = s.dm.grad_phi_sp
         state["grad_phi_fv"] = s.dm.grad_phi_fv

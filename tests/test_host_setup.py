@@ -55,7 +55,8 @@ def test_initial_state_matches_reference(name):
     lims = [kw.get(f"{d}lim", (0, 1)) for d in DIMS[:ndim]]
     ops = golden_operators(data)
     W_gh, W_init_cv, W_sp, U_sp, U_cv = initial_state(ndim, list(kw["N"]), kw["p"], lims, make_ic(meta["ic"]),
-                                                      ops, kw.get("gamma", 1.4))
+                                                      ops, kw.get("gamma", 1.4),
+                                                      isothermal=kw.get("isothermal", False))
     assert same(W_init_cv, data["init_W_cv"])
     assert same(U_sp, data["init_U_sp"])
     assert same(U_cv, data["init_U_cv"])
@@ -71,8 +72,7 @@ def test_subcell_faces_mirror_ghosts():
 
 
 def test_unsupported_options_raise():
-    for kw in ({"viscosity": True, "update": "FV", "FB": True}, {"WB": True}, {"isothermal": True},
-               {"predictor": False}):
+    for kw in ({"viscosity": True, "update": "FV", "FB": True}, {"WB": True}, {"predictor": False}):
         with pytest.raises(NotImplementedError):
             SDADER_Simulator(N=(4,), **kw)
     with pytest.raises(AttributeError):
