@@ -193,12 +193,14 @@ def compulsory_bytes_per_cell_step(D, p):
 # capture, --clock-control none -k regex:k_interior over the four launches of
 # one step, metrics dram__bytes_read.sum, dram__bytes_write.sum,
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, of
-# `python bench.py --cells N --steps 1 --warmup 1 --no-cpu-baseline`, divided
-# by the N^2 cells (both scale with the cell count; the full 512^2 workload
-# is not captured with more than one pass).  Keyed by (D, p, update, build).
+# `python bench.py --lean --cells 256 --steps 1 --warmup 1 [--build fma]`,
+# divided by the 65,536 cells (both scale with the cell count, and h = 1/256
+# is a power of two as at 512^2, so the derivative takes the same
+# prescaled form; the full 512^2 workload is not captured with more than
+# one pass).  Keyed by (D, p, update, build).
 NCU_K_INTERIOR = {
-    (2, 3, "FV", "ieee"): {"cells_captured": 256 * 256, "dram_bytes": 4 * 448.170496e6 / 65536,
-                           "fp64_inst": 42966.0},
+    (2, 3, "FV", "ieee"): {"cells_captured": 256 * 256, "dram_bytes": 12095.8 + 14246.0, "fp64_inst": 43330.0},
+    (2, 3, "FV", "fma"): {"cells_captured": 256 * 256, "dram_bytes": 12134.0 + 14250.6, "fp64_inst": 29938.0},
 }
 
 
@@ -610,6 +612,11 @@ def fma_build_section(args, kw, s_ieee, stream, dof, cells, fp64, ieee_ms_step):
             kint[1] / 1e3) / 1e12
         roof = {"kernel": "k_interior", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                 "frac": achieved / fp64 if fp64 else None, "avg_launch_ms": kint[1] / kint[0]}
+        ncu = NCU_K_INTERIOR.get((D, p, kw.get("update", "SD"), "fma"))
+        if ncu and fp64:
+            rate = ncu["fp64_inst"] * cells * prof_steps / (kint[1] / 1e3)
+            roof["fp64_issue_frac"] = rate / (fp64 * 1e12 / 2.0)
+            roof["fp64_instructions_per_cell_step"] = ncu["fp64_inst"]
     f.close()
     # deviation from the product build over 10 steps from one initial state
     # (fresh simulators: the FV boundary buffers start from the initial

@@ -24,6 +24,17 @@ def case_names():
                   if not p.endswith("operators.npz"))
 
 
+def adjoint_case_names():
+    """The golden cases the adjoint covers: not viscosity, gravity or the
+    isothermal system (spd_adjoint_enable refuses those)."""
+    out = []
+    for name in case_names():
+        kw = load(name)[1]
+        if not (kw.get("viscosity") or kw.get("potential") or kw.get("isothermal")):
+            out.append(name)
+    return out
+
+
 def load_long(name):
     """A long-horizon fixture: as ``load``; ``meta["run"]`` is {"steps": n}
     or {"t_end": t}, and the arrays hold the dt of every step and, with

@@ -16,6 +16,14 @@ def product_from_golden(data, kw, meta):
     # before recomputing it from U_sp (FV) or at the end of a run (SD)
     s.dm.U_cv = data["init_U_cv"] if "init_U_cv" in data else s.compute_conservatives(data["init_W_cv"])
     s.dm.W_cv = data["init_W_cv"]
+    # the stored boundary arrays of the reference's run (the "ic", "eq" and
+    # "pressure" sides read them; made here they would carry this machine's
+    # einsum roundings)
+    for d in s.dims:
+        if f"init_BC_fp_{d}" in data:
+            s._ctx.upload(f"BC_fp_{d}", data[f"init_BC_fp_{d}"])
+        if f"init_BC_fv_{d}" in data and s.update == "FV":
+            s._ctx.upload(f"BC_fv_{d}", data[f"init_BC_fv_{d}"])
     if kw.get("potential", False):
         s.dm.grad_phi_sp = data["grad_phi_sp"]
         s.dm.grad_phi_fv = data["grad_phi_fv"]

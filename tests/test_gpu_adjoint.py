@@ -13,7 +13,7 @@ spd_gb300.adjoint.SDADERSteps) against two references:
 import numpy as np
 import pytest
 
-from golden_cases import case_names, load, oracle_from_golden
+from golden_cases import adjoint_case_names, case_names, load, oracle_from_golden
 from gpu_helpers import product_from_golden
 
 pytestmark = pytest.mark.gpu
@@ -45,7 +45,7 @@ def _steps_for(meta):
     return min(int(meta["steps"]), 2)
 
 
-@pytest.mark.parametrize("name", case_names())
+@pytest.mark.parametrize("name", adjoint_case_names())
 def test_vjp_matches_torch_autograd(name):
     data, kw, meta = load(name)
     nsteps = _steps_for(meta)
@@ -143,7 +143,7 @@ def _fd_check(s, U0, nsteps, ndir, eps, seed):
     return errs
 
 
-@pytest.mark.parametrize("name", case_names())
+@pytest.mark.parametrize("name", adjoint_case_names())
 def test_vjp_matches_central_differences(name):
     data, kw, meta = load(name)
     s = product_from_golden(data, kw, meta)
