@@ -186,9 +186,10 @@ int spd_launch_count(const spd_ctx* ctx, long long* count);
 int spd_destroy(spd_ctx* ctx);
 /* CFL time step dt = cfl_coeff * (h / max(ndim*c_s + sum |v|)) from
  * primitive subcell averages already on the device, without allocating
- * device memory.  No counterpart in the reference: it serves callers that
- * must not call cudaMalloc (graph capture, a framework allocator that owns
- * device memory, allocation-free real-time loops).  W_cv_dev holds
+ * device memory (the inviscid limit; the viscous one of compute_dt is not
+ * applied).  No counterpart in the reference: it serves callers that must
+ * not call cudaMalloc -- a host framework whose allocator owns all device
+ * memory, real-time loops that forbid allocation after start-up.  W_cv_dev holds
  * ndim + 2 variables one after the other, n_subcells values each (any
  * subcell order); h = h_min / (p + 1); dt_dev receives one double; the
  * work is queued on ``stream`` (a cudaStream_t, NULL = default stream).

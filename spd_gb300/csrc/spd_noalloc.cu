@@ -1,10 +1,10 @@
 // CFL time step from device-resident primitive subcell averages, without
 // any device allocation.
 //
-// Who needs this: callers that may not call cudaMalloc -- code that records
-// a CUDA graph (allocation is not capturable), solvers embedded in a host
-// framework whose caching allocator owns all device memory, and real-time
-// loops that forbid allocation after start-up.  They hand in their own
+// Who needs this: callers that may not call cudaMalloc -- solvers embedded
+// in a host framework whose caching allocator owns all device memory, and
+// real-time loops that forbid allocation after start-up.  The dt is the
+// inviscid CFL limit (compute_dt's viscous limit is not applied).  They hand in their own
 // input and output buffers; the only scratch this entry point uses is the
 // fixed array below, which lives in the library image.
 //

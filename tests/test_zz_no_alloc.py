@@ -1,8 +1,8 @@
 """The allocation-free CFL entry point (spd_cfl_dt_noalloc).
 
-Some callers cannot call cudaMalloc: code being recorded into a CUDA graph,
-hosts whose framework allocator owns all device memory, and real-time loops
-that forbid allocation after start-up.  spd_cfl_dt_noalloc serves them with
+Some callers cannot call cudaMalloc: hosts whose framework allocator owns
+all device memory, and real-time loops that forbid allocation after
+start-up.  spd_cfl_dt_noalloc serves them with
 a fixed scratch array inside the library; this test checks, through the C
 ABI, that it returns the same dt as the context's own compute_dt, bit for
 bit (the tolerance of every parity test here), on two calls in a row.
