@@ -79,6 +79,19 @@ int ensure_staging(spd_ctx* C, size_t count) {
   return 0;
 }
 
+// Device address of a host buffer the GPU can read and write directly
+// (pinned or registered host memory, reached over NVLink-C2C on GB300), or
+// null for any other pointer (pageable host memory, device memory).
+const double* device_alias(const double* host) {
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type != cudaMemoryTypeHost || attr.devicePointer == nullptr) return nullptr;
+  return static_cast<const double*>(attr.devicePointer);
+}
+
 long long n_faces_host(const Geo& g, int d) {
   return (long long)(g.X[0] + (d == 0)) * (g.X[1] + (d == 1)) * (g.X[2] + (d == 2));
 }
@@ -486,11 +499,17 @@ int spd_upload(spd_ctx* C, int field, const double* host, size_t count) {
   if (need == 0 || count != need) return fail(C, SPD_ERR_ARG, "upload: wrong field or element count");
   const Geo& g = C->geo;
   if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV || field == SPD_U_SP_ADJ) {
-    if (int r = ensure_staging(C, need)) return r;
-    CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyDefault, C->stream));
     double* dst = (field == SPD_U_SP) ? C->U_sp
                   : (field == SPD_U_CV ? C->U_cv : (field == SPD_W_CV ? C->W_cv : C->Usp_a));
-    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, C->staging, dst, 1,
+    // pinned host buffers are read by the layout kernel itself (one pass
+    // over the host link); any other pointer goes through a device copy
+    const double* src = device_alias(host);
+    if (!src) {
+      if (int r = ensure_staging(C, need)) return r;
+      CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyDefault, C->stream));
+      src = C->staging;
+    }
+    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, src, dst, 1,
                                                                        (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
     CKL();
     CK(cudaStreamSynchronize(C->stream));
@@ -541,11 +560,18 @@ int spd_download(spd_ctx* C, int field, double* host, size_t count) {
   if (need == 0 || count != need) return fail(C, SPD_ERR_ARG, "download: wrong field or element count");
   const Geo& g = C->geo;
   if (field == SPD_U_SP || field == SPD_U_CV || field == SPD_W_CV || field == SPD_U_SP_ADJ) {
-    if (int r = ensure_staging(C, need)) return r;
     const double* src = (field == SPD_U_SP) ? C->U_sp
                         : (field == SPD_U_CV ? C->U_cv : (field == SPD_W_CV ? C->W_cv : C->Usp_a));
-    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(
-        g, C->D, C->n, C->V, src, C->staging, 0, (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
+    const int fv = (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1;
+    // pinned host buffers are written by the layout kernel itself
+    if (double* dst = const_cast<double*>(device_alias(host))) {
+      k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, src, dst, 0, fv);
+      CKL();
+      CK(cudaStreamSynchronize(C->stream));
+      return SPD_OK;
+    }
+    if (int r = ensure_staging(C, need)) return r;
+    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, src, C->staging, 0, fv);
     CKL();
     CK(cudaMemcpyAsync(host, C->staging, need * sizeof(double), cudaMemcpyDefault, C->stream));
     CK(cudaStreamSynchronize(C->stream));
