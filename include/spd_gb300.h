@@ -87,7 +87,30 @@ enum spd_field {
    * (compute_cv_from_sp of the former; the reference keeps them transposed
    * to the FV layout) */
   SPD_GRAD_PHI_SP = 18,
-  SPD_GRAD_PHI_CV = 19
+  SPD_GRAD_PHI_CV = 19,
+  /* write-only, with WB: the equilibrium of the well-balanced mode
+   * (src/sdader_simulator.py:436-481), in the reference's layouts --
+   * U_eq_sp (SD layout), U_eq_cv (cell averages, SD layout), per direction
+   * M_eq_fp / F_eq_fp (conservative state and flux at the flux points,
+   * (V, cells..., points...) with p+2 points along the direction), with the
+   * FV update per direction M_eq_faces / F_eq_faces (primitive state and
+   * flux at the subcell faces, FV face layout) and M_eq_fv (primitives on
+   * the subcell grid with 2 ghost layers) */
+  SPD_U_EQ_SP = 20,
+  SPD_U_EQ_CV = 21,
+  SPD_M_EQ_FP_X = 22,
+  SPD_M_EQ_FP_Y = 23,
+  SPD_M_EQ_FP_Z = 24,
+  SPD_F_EQ_FP_X = 25,
+  SPD_F_EQ_FP_Y = 26,
+  SPD_F_EQ_FP_Z = 27,
+  SPD_M_EQ_FACES_X = 28,
+  SPD_M_EQ_FACES_Y = 29,
+  SPD_M_EQ_FACES_Z = 30,
+  SPD_F_EQ_FACES_X = 31,
+  SPD_F_EQ_FACES_Y = 32,
+  SPD_F_EQ_FACES_Z = 33,
+  SPD_M_EQ_FV = 34
 };
 
 /* Constructor options of SDADER_Simulator (src/simulator.py:10-36,
@@ -126,6 +149,9 @@ typedef struct spd_config {
   int potential;
   /* isothermal system (src/hydro.py:84,123,169, src/riemann_solver.py:142,210) */
   int isothermal;
+  /* well-balanced mode (src/sdader_simulator.py:361-378 and callees): the
+   * step advances U - U_eq; the equilibrium arrays by spd_upload */
+  int WB;
 } spd_config;
 
 /* Constant operators built at setup on the host

@@ -513,7 +513,7 @@ class OracleSDADER:
                  riemann_solver_sd, riemann_solver_fv, slope_limiter, update,
                  FB, tolerance, SED, NAD, PAD, blending, min_rho, max_rho,
                  min_P, godunov, ops, state, Nghc=2, viscosity=False, nu=1e-4, beta=2.0 / 3, potential=False,
-                 isothermal=False):
+                 isothermal=False, WB=False):
         self.ndim = ndim
         self.N = list(N)          # cells per dim, x first
         self.p = p
@@ -569,6 +569,24 @@ class OracleSDADER:
         if potential:
             self.grad_phi_sp = conv(state["grad_phi_sp"])
             self.grad_phi_fv = conv(state["grad_phi_fv"])
+        # well-balanced mode (src/sdader_simulator.py:436-481): the step
+        # advances the perturbation U - U_eq; equilibrium states at the
+        # solution points (U_eq_sp), as subcell averages (U_eq_cv, SD
+        # layout), at the flux points of each direction with matched
+        # element-interface values (M_eq_fp, conservative) and their fluxes
+        # (F_eq_fp); with the FV update the primitive equilibrium at the
+        # subcell faces (M_eq_faces) with its fluxes and on the extended
+        # subcell grid (M_eq_fv)
+        self.WB = WB
+        if WB:
+            self.U_eq_sp = conv(state["U_eq_sp"])
+            self.U_eq_cv = conv(state["U_eq_cv"])
+            self.M_eq_fp = {i: conv(state[f"M_eq_fp_{DIMS[i]}"]) for i in range(ndim)}
+            self.F_eq_fp = {i: conv(state[f"F_eq_fp_{DIMS[i]}"]) for i in range(ndim)}
+            if update == "FV":
+                self.M_eq_faces = {i: conv(state[f"M_eq_faces_{DIMS[i]}"]) for i in range(ndim)}
+                self.F_eq_faces = {i: conv(state[f"F_eq_faces_{DIMS[i]}"]) for i in range(ndim)}
+                self.M_eq_fv = conv(state["M_eq_fv"])
         self.BC_fp = {i: conv(state[f"BC_fp_{DIMS[i]}"]) for i in range(ndim) if f"BC_fp_{DIMS[i]}" in state}
         self.BC_fv = {}
         for i in range(ndim):
@@ -641,6 +659,9 @@ class OracleSDADER:
             ax_sp = sp_axis(nd, idim)
             ax_cell = cell_axis(nd, idim)
             M_fp = apply_axis(ops["sp_to_fp"], U_ader, ax_sp, axis_order(idim))
+            if self.WB:
+                # U' -> U at the flux points (src/sdader_simulator.py:221-223)
+                M_fp = M_fp + xp.expand(self.M_eq_fp[idim], 1)
             # interior flux points (the edge values are replaced below)
             M_in = _shift(M_fp, 1, -1, ax_sp)
             F_in = compute_fluxes(compute_primitives(M_in, nd, self.gamma, iso=self.iso), vels, self.gamma, self.iso)
@@ -648,6 +669,9 @@ class OracleSDADER:
             F = riemann(self.rs_sd, ML, MR, vels, self.gamma, self.min_c2, prims=False, iso=self.iso)
             F_all[idim] = xp.cat([xp.expand(_shift(F, None, -1, ax_cell + 1), ax_sp), F_in,
                                   xp.expand(_shift(F, 1, None, ax_cell + 1), ax_sp)], ax_sp)
+            if self.WB:
+                # F -> F' (src/sdader_simulator.py:235-237)
+                F_all[idim] = F_all[idim] - xp.expand(self.F_eq_fp[idim], 1)
             M_all[idim] = M_fp
         if self.viscosity:
             F_all = self.add_viscosity(M_all, F_all)
@@ -909,8 +933,8 @@ class OracleSDADER:
         nd = self.ndim
         U_cv = xp.detach(U_cv)
         U_new = xp.detach(U_new)
-        W_old = compute_primitives(U_cv, nd, self.gamma, iso=self.iso)
-        W_new = compute_primitives(U_new, nd, self.gamma, iso=self.iso)
+        W_old = self.prims_cv(U_cv)
+        W_new = self.prims_cv(U_new)
         M = self.fv_boundaries(self.pad(W_old))
         act = (slice(None),) + (slice(g, -g),) * nd
         center = M[act]
@@ -944,6 +968,8 @@ class OracleSDADER:
         _p_ = nd + 1
         troubles = xp.f64(xp.maximum(pt[0], pt[_p_]))
         if self.PAD:
+            if self.WB:
+                W_new = W_new + compute_primitives(self.to_fv(self.U_eq_cv), nd, self.gamma, iso=self.iso)
             troubles = xp.where(W_new[0] >= self.min_rho, troubles, 1.0)
             troubles = xp.where(W_new[0] <= self.max_rho, troubles, 1.0)
             troubles = xp.where(W_new[_p_] >= self.min_P, troubles, 1.0)
@@ -1043,8 +1069,15 @@ class OracleSDADER:
             crop = [slice(None)] + [slice(1, -1)] * nd
             crop[ax] = slice(None)
             dMhs[idim] = dMh[tuple(crop)]
+            if self.WB:
+                # gradients of the equilibrium (src/muscl.py:203-204)
+                dMhs[idim + nd] = limited_gradient(self.M_eq_fv, hcv, hfp, ax, self.limiter)[tuple(crop)]
         inner = (slice(None),) + (slice(1, -1),) * nd
-        W = M[inner]
+        if self.WB:
+            Mfull = M + self.M_eq_fv           # src/muscl.py:205-206
+            W = Mfull[inner]
+        else:
+            W = M[inner]
         _p_ = nd + 1
         vels = self.vels()
         dtW = {}
@@ -1059,10 +1092,27 @@ class OracleSDADER:
                 sub(0, W[vel] * dW[0] + W[0] * dW[vel])
                 sub(_p_, W[vel] * dW[_p_] + self.gamma * W[_p_] * dW[vel])
                 sub(vel, W[vel] * dW[vel] + dW[_p_] / W[0])
+            if self.WB:
+                # src/muscl.py:167-170; the transverse terms below then take
+                # the equilibrium gradient, as the reference's reassigned dW
+                dW = dMhs[idim + nd]
+                sub(0, W[vel] * dW[0])
+                sub(_p_, W[vel] * dW[_p_])
             for vel2 in vels[1:]:
                 sub(vel2, W[vel] * dW[vel2])
         dtW[_p_] = dtW[_p_] * 0
-        pred = self._embed(M, W + 0.5 * xp.stack([dtW[v] for v in range(nd + 2)], 0) * dt)
+        if self.WB:
+            if self.potential:
+                # src/muscl.py:208-212, on the active subcells only
+                act = (slice(None),) * 0 + (slice(1, -1),) * nd
+                with np.errstate(all="ignore"):
+                    drho = ((Mfull[0] - self.M_eq_fv[0]) / Mfull[0])[inner[1:]]
+                for vel in vels:
+                    t = xp.copy(dtW[vel])
+                    t[act] = t[act] + drho[act] * self.grad_phi_fv[vel - 1]
+                    dtW[vel] = t
+            M = Mfull - self.M_eq_fv           # src/muscl.py:214
+        pred = self._embed(M, M[inner] + 0.5 * xp.stack([dtW[v] for v in range(nd + 2)], 0) * dt)
         F = {}
         for idim in range(nd):
             ax = nd - idim
@@ -1074,8 +1124,14 @@ class OracleSDADER:
             crop_m[ax] = slice(1, -g)
             crop_s[ax] = slice(None, -1)
             ML = pred[tuple(crop_m)] + S[idim][tuple(crop_s)]
+            if self.WB:
+                # src/fv_simulator.py:150-154
+                MR = MR + self.M_eq_faces[idim]
+                ML = ML + self.M_eq_faces[idim]
             F[idim] = riemann(self.rs_fv, ML, MR, self.rolled_vels(idim), self.gamma,
                               self.min_c2, prims=True, iso=self.iso)
+            if self.WB:
+                F[idim] = F[idim] - self.F_eq_faces[idim]     # src/fv_simulator.py:163-165
         return F
 
     def _embed(self, M, inner):
@@ -1099,7 +1155,7 @@ class OracleSDADER:
         Ffaces = self.integrate_faces(F_all)
         w = self.ops["w_tp"]
         for i in range(self.T):
-            W_cv = compute_primitives(U_cv, nd, self.gamma, iso=self.iso)
+            W_cv = self.prims_cv(U_cv)
             dt = self.dt * w[i]
             F_HO = self.store_high_order_fluxes(Ffaces, i)
             U_new = self.fv_apply_fluxes(U_cv, F_HO, dt)
@@ -1123,13 +1179,29 @@ class OracleSDADER:
         self.U_sp = apply_full(self.ops["cv_to_sp"], self.U_cv, nd, rows=True)
 
     # ---- drivers (src/sdader_simulator.py:361-413) -----------------------
+    def prims_cv(self, U):
+        """src/sdader_simulator.py:351-356 on an FV-layout array: with WB the
+        primitive perturbation prim(U + U_eq) - prim(U_eq)."""
+        if self.WB:
+            Ueq = self.to_fv(self.U_eq_cv)
+            return (compute_primitives(U + Ueq, self.ndim, self.gamma, iso=self.iso)
+                    - compute_primitives(Ueq, self.ndim, self.gamma, iso=self.iso))
+        return compute_primitives(U, self.ndim, self.gamma, iso=self.iso)
+
     def perform_update(self):
         self.n_step += 1
+        if self.WB:
+            self.U_sp = self.U_sp - self.U_eq_sp
         F_all = self.ader_predictor()
         if self.update == "SD":
             self.ader_update(F_all)
         else:
             self.fv_update(F_all)
+        if self.WB:
+            # src/sdader_simulator.py:372-375; with the SD update U_cv is the
+            # previous step's (the SD update does not recompute it)
+            self.U_sp = self.U_sp + self.U_eq_sp
+            self.U_cv = self.U_cv + self.U_eq_cv
         self.W_cv = compute_primitives(self.U_cv, self.ndim, self.gamma, iso=self.iso)
         self.time += self.dt
 

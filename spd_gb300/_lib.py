@@ -28,6 +28,9 @@ FIELD = {
     "BC_fv_x": 11, "BC_fv_y": 12, "BC_fv_z": 13, "U_sp_adj": 14,
     "F_faces_x": 15, "F_faces_y": 16, "F_faces_z": 17,
     "grad_phi_sp": 18, "grad_phi_cv": 19,
+    "U_eq_sp": 20, "U_eq_cv": 21, "M_eq_fp_x": 22, "M_eq_fp_y": 23, "M_eq_fp_z": 24,
+    "F_eq_fp_x": 25, "F_eq_fp_y": 26, "F_eq_fp_z": 27, "M_eq_faces_x": 28, "M_eq_faces_y": 29,
+    "M_eq_faces_z": 30, "F_eq_faces_x": 31, "F_eq_faces_y": 32, "F_eq_faces_z": 33, "M_eq_fv": 34,
 }
 
 # every entry point declared in include/spd_gb300.h
@@ -75,6 +78,7 @@ class spd_config(ctypes.Structure):
         ("beta", ctypes.c_double),
         ("potential", ctypes.c_int),
         ("isothermal", ctypes.c_int),
+        ("WB", ctypes.c_int),
     ]
 
 

@@ -41,9 +41,10 @@ extern "C" {
 
 int spd_adjoint_enable(spd_ctx* C, int depth) {
   if (!C || depth < 1) return SPD_ERR_ARG;
-  if (C->cfg.viscosity || C->cfg.potential || C->cfg.isothermal)
+  if (C->cfg.viscosity || C->cfg.potential || C->cfg.isothermal || C->cfg.WB)
     return fail(C, SPD_ERR_ARG,
-                "the adjoint does not differentiate the viscous fluxes, the gravity source or the isothermal system");
+                "the adjoint does not differentiate the viscous fluxes, the gravity source, the isothermal "
+                "system or the well-balanced mode");
   if (C->adj_depth >= depth) return SPD_OK;
   adj_free(C);
   const Geo& g = C->geo;
@@ -128,9 +129,10 @@ int spd_record_step(spd_ctx* C, int slot, double dt) {
 
 int spd_tape_enable(spd_ctx* C, int nsteps) {
   if (!C || nsteps < 1) return SPD_ERR_ARG;
-  if (C->cfg.viscosity || C->cfg.potential || C->cfg.isothermal)
+  if (C->cfg.viscosity || C->cfg.potential || C->cfg.isothermal || C->cfg.WB)
     return fail(C, SPD_ERR_ARG,
-                "decision tapes do not cover the viscous fluxes, the gravity source or the isothermal system");
+                "decision tapes do not cover the viscous fluxes, the gravity source, the isothermal system or "
+                "the well-balanced mode");
   if (C->tape_steps >= nsteps) return SPD_OK;
   if (C->stream) cudaStreamSynchronize(C->stream);
   for (void* p : C->tape_allocs) cudaFree(p);

@@ -136,7 +136,7 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
                 "viscosity with the FV update and FB: the reference's viscous fallback fluxes raise "
                 "AttributeError (src/muscl.py:253 calls compute_slopes, which calls a missing method)");
   if (cfg->viscosity && !(cfg->nu >= 0.0)) return fail(C, SPD_ERR_ARG, "nu must be >= 0");
-  if (cfg->update == SPD_UPDATE_FV && cfg->FB) {
+  if (cfg->update == SPD_UPDATE_FV && cfg->FB && !cfg->WB) {
     // src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros (the
     // perturbation of the well-balanced mode, which is not implemented), so
     // the reference's fallback flux at those faces is 0*NaN and its first
@@ -292,6 +292,31 @@ int spd_create(const spd_config* cfg, const spd_operators* ops, spd_ctx** out) {
     if (int r = dalloc(C, &C->Fi[d], (size_t)V * T * NJ * nI)) return r;
     if (int r = dalloc(C, &C->bcfix[d], (size_t)2 * V * NJ * (Nc / g.N[d]))) return r;
     CK(cudaMemset(C->bcfix[d], 0, sizeof(double) * 2 * V * NJ * (Nc / g.N[d])));
+  }
+  if (cfg->WB) {
+    if (int r = dalloc(C, &C->Ueq_sp, (size_t)V * NS * Nc)) return r;
+    if (int r = dalloc(C, &C->Ueq_cv, (size_t)V * Nq)) return r;
+    if (int r = dalloc(C, &C->Weq_cv, (size_t)V * Nq)) return r;
+    CK(cudaMemset(C->Ueq_sp, 0, sizeof(double) * V * NS * Nc));
+    CK(cudaMemset(C->Ueq_cv, 0, sizeof(double) * V * Nq));
+    CK(cudaMemset(C->Weq_cv, 0, sizeof(double) * V * Nq));
+    for (int d = 0; d < D; ++d) {
+      if (int r = dalloc(C, &C->Meq_fp[d], (size_t)V * NJ * nf * Nc)) return r;
+      if (int r = dalloc(C, &C->Feq_fp[d], (size_t)V * NJ * nf * Nc)) return r;
+      CK(cudaMemset(C->Meq_fp[d], 0, sizeof(double) * V * NJ * nf * Nc));
+      CK(cudaMemset(C->Feq_fp[d], 0, sizeof(double) * V * NJ * nf * Nc));
+      if (cfg->update == SPD_UPDATE_FV) {
+        const long long nfc = n_faces_host(g, d);
+        if (int r = dalloc(C, &C->Meq_faces[d], (size_t)V * nfc)) return r;
+        if (int r = dalloc(C, &C->Feq_faces[d], (size_t)V * nfc)) return r;
+        CK(cudaMemset(C->Meq_faces[d], 0, sizeof(double) * V * nfc));
+        CK(cudaMemset(C->Feq_faces[d], 0, sizeof(double) * V * nfc));
+      }
+    }
+    if (cfg->update == SPD_UPDATE_FV) {
+      if (int r = dalloc(C, &C->Meq_fv, (size_t)V * Nqe)) return r;
+      CK(cudaMemset(C->Meq_fv, 0, sizeof(double) * V * Nqe));
+    }
   }
   if (cfg->potential) {
     if (int r = dalloc(C, &C->gphi_sp, (size_t)D * NS * Nc)) return r;
@@ -460,6 +485,27 @@ static size_t field_count(spd_ctx* C, int field) {
     }
     case SPD_GRAD_PHI_SP:
     case SPD_GRAD_PHI_CV: return C->gphi_sp ? (size_t)D * C->NS * g.Nc : 0;
+    case SPD_U_EQ_SP:
+    case SPD_U_EQ_CV: return C->Ueq_sp ? (size_t)V * C->NS * g.Nc : 0;
+    case SPD_M_EQ_FP_X:
+    case SPD_M_EQ_FP_Y:
+    case SPD_M_EQ_FP_Z:
+    case SPD_F_EQ_FP_X:
+    case SPD_F_EQ_FP_Y:
+    case SPD_F_EQ_FP_Z: {
+      const int d = (field - SPD_M_EQ_FP_X) % 3;
+      return (d < D && C->Meq_fp[d]) ? (size_t)V * C->NJ * C->nf * g.Nc : 0;
+    }
+    case SPD_M_EQ_FACES_X:
+    case SPD_M_EQ_FACES_Y:
+    case SPD_M_EQ_FACES_Z:
+    case SPD_F_EQ_FACES_X:
+    case SPD_F_EQ_FACES_Y:
+    case SPD_F_EQ_FACES_Z: {
+      const int d = (field - SPD_M_EQ_FACES_X) % 3;
+      return (d < D && C->Meq_faces[d]) ? (size_t)V * n_faces_host(g, d) : 0;
+    }
+    case SPD_M_EQ_FV: return C->Meq_fv ? (size_t)V * g.Nqe : 0;
     case SPD_F_FACES_X:
     case SPD_F_FACES_Y:
     case SPD_F_FACES_Z: {
@@ -513,6 +559,55 @@ int spd_upload(spd_ctx* C, int field, const double* host, size_t count) {
                                                                        (field == SPD_U_SP || field == SPD_U_SP_ADJ) ? 0 : 1);
     CKL();
     CK(cudaStreamSynchronize(C->stream));
+    return SPD_OK;
+  }
+  if (field == SPD_U_EQ_SP || field == SPD_U_EQ_CV) {
+    if (int r = ensure_staging(C, need)) return r;
+    CK(cudaMemcpyAsync(C->staging, host, need * sizeof(double), cudaMemcpyDefault, C->stream));
+    double* dst = (field == SPD_U_EQ_SP) ? C->Ueq_sp : C->Ueq_cv;
+    k_sd_layout<<<blocks_for((long long)need, BS), BS, 0, C->stream>>>(g, C->D, C->n, C->V, C->staging, dst, 1,
+                                                                       field == SPD_U_EQ_SP ? 0 : 1);
+    CKL();
+    // the equilibrium's primitives (src/trouble_detection.py:59-60,
+    // src/sdader_simulator.py:351-356 compute them from U_eq_cv)
+    if (field == SPD_U_EQ_CV)
+      if (int r = C->stepper->eq_prims(C)) return r;
+    CK(cudaStreamSynchronize(C->stream));
+    return SPD_OK;
+  }
+  if (field >= SPD_M_EQ_FP_X && field <= SPD_F_EQ_FP_Z) {
+    // reference (V, cells z..x, points z..x), p+2 points along d -> [v][j][f][cell]
+    const int d = (field - SPD_M_EQ_FP_X) % 3;
+    double* dst = (field <= SPD_M_EQ_FP_Z) ? C->Meq_fp[d] : C->Feq_fp[d];
+    const int n = C->n, nf = C->nf, NJ = C->NJ, V = C->V, D = C->D;
+    std::vector<double> tmp(need);
+    int np[3] = {1, 1, 1};
+    for (int e = 0; e < D; ++e) np[e] = (e == d) ? nf : n;
+    size_t r = 0;
+    for (int v = 0; v < V; ++v)
+      for (int cz = 0; cz < g.N[2]; ++cz)
+        for (int cy = 0; cy < g.N[1]; ++cy)
+          for (int cx = 0; cx < g.N[0]; ++cx)
+            for (int kz = 0; kz < np[2]; ++kz)
+              for (int ky = 0; ky < np[1]; ++ky)
+                for (int kx = 0; kx < np[0]; ++kx) {
+                  const int k[3] = {kx, ky, kz};
+                  int j = 0;
+                  if (d == 0) j = ky + n * kz;
+                  else if (d == 1) j = kx + n * kz;
+                  else j = kx + n * ky;
+                  const long long c = cx + (long long)g.N[0] * (cy + (long long)g.N[1] * cz);
+                  tmp[(((size_t)v * NJ + j) * nf + k[d]) * g.Nc + c] = host[r++];
+                }
+    CK(cudaMemcpy(dst, tmp.data(), need * sizeof(double), cudaMemcpyHostToDevice));
+    return SPD_OK;
+  }
+  if (field >= SPD_M_EQ_FACES_X && field <= SPD_M_EQ_FV) {
+    // the FV face and extended layouts are the reference's C order
+    double* dst = (field == SPD_M_EQ_FV) ? C->Meq_fv
+                  : (field <= SPD_M_EQ_FACES_Z ? C->Meq_faces[field - SPD_M_EQ_FACES_X]
+                                               : C->Feq_faces[field - SPD_F_EQ_FACES_X]);
+    CK(cudaMemcpy(dst, host, need * sizeof(double), cudaMemcpyHostToDevice));
     return SPD_OK;
   }
   if (field == SPD_GRAD_PHI_SP || field == SPD_GRAD_PHI_CV) {

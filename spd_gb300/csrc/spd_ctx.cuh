@@ -95,6 +95,16 @@ struct spd_ctx {
   // [d][subcell] as subcell averages (FV layout)
   double* gphi_sp = nullptr;
   double* gphi_fv = nullptr;
+  // well-balanced mode: equilibrium U_eq_sp [v][s][cell]; U_eq_cv and its
+  // primitives [v][subcell]; per direction the conservative state and flux
+  // at the flux points [v][j][f][cell]; with the FV update the primitive
+  // state and flux at the subcell faces [v][face] and the primitives on the
+  // extended subcell grid [v][ext]
+  double *Ueq_sp = nullptr, *Ueq_cv = nullptr, *Weq_cv = nullptr, *Meq_fv = nullptr;
+  double* Meq_fp[3] = {nullptr, nullptr, nullptr};
+  double* Feq_fp[3] = {nullptr, nullptr, nullptr};
+  double* Meq_faces[3] = {nullptr, nullptr, nullptr};
+  double* Feq_faces[3] = {nullptr, nullptr, nullptr};
   // FV scratch
   double* F_HO[3] = {nullptr, nullptr, nullptr};
   double *ext_old = nullptr, *ext_new = nullptr, *theta_src = nullptr, *theta_a = nullptr, *theta_b = nullptr;
@@ -235,6 +245,7 @@ struct StepperBase {
   virtual int sp_to_cv(spd_ctx* C) = 0;  // U_cv = sp_to_cv(U_sp)
   virtual int configure(spd_ctx* C) = 0;
   virtual int vjp(spd_ctx* C) = 0;       // Usp_a <- (d U_sp_new / d U_sp)^T Usp_a of the recorded step
+  virtual int eq_prims(spd_ctx* C) = 0;  // Weq_cv = prim(Ueq_cv) (well-balanced mode)
   int cpb = 32;       // cells per block of k_interior (a power of two <= max_cpb)
   int max_cpb = 32;   // largest cpb whose shared-memory tile fits
   size_t smem = 0;

@@ -89,6 +89,25 @@ __device__ __forceinline__ void potential_source(const Geo& g, const double* __r
   }
 }
 
+// Primitives of one subcell's state (src/sdader_simulator.py:351-356): in
+// the well-balanced mode (Ueq non-null) the perturbation
+// prim(U + U_eq) - prim(U_eq), with prim(U_eq) given as Weq; [v][subcell]
+template <int D>
+__device__ __forceinline__ void prims_cv(const Geo& g, const double* u, double* W, const double* __restrict__ Ueq,
+                                         const double* __restrict__ Weq, long long q) {
+  constexpr int V = D + 2;
+  if (Ueq == nullptr) {
+    prim<D>(u, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+    return;
+  }
+  double uf[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) uf[v] = u[v] + Ueq[(long long)v * g.Nq + q];
+  prim<D>(uf, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+#pragma unroll
+  for (int v = 0; v < V; ++v) W[v] = W[v] - Weq[(long long)v * g.Nq + q];
+}
+
 // dUdt of one subcell from the face fluxes (src/fv_simulator.py:189-205)
 template <int D>
 __device__ __forceinline__ void flux_divergence(const Geo& g, const FvGeo& fg, int ix, int iy, int iz,
@@ -121,7 +140,8 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
                                            double w_i, const double* F0, const double* F1, const double* F2,
                                            const double* __restrict__ U_cv, double* __restrict__ U_new,
                                            double* ext_old, double* ext_new, int write_ext,
-                                           const double* __restrict__ gphi) {
+                                           const double* __restrict__ gphi, const double* __restrict__ Ueq,
+                                           const double* __restrict__ Weq) {
   constexpr int V = D + 2;
   const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nq) return;
@@ -147,11 +167,11 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
 #pragma unroll
       for (int v = 0; v < V; ++v) W[v] = ext_new[(long long)v * g.Nqe + e];
     } else {
-      prim<D>(u, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+      prims_cv<D>(g, u, W, Ueq, Weq, q);
     }
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_old[(long long)v * g.Nqe + e] = W[v];
-    prim<D>(un, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+    prims_cv<D>(g, un, W, Ueq, Weq, q);
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
   }
@@ -161,8 +181,10 @@ template <int D>
 __global__ void k_fv_candidate(Geo g, FvGeo fg, const double* __restrict__ dt_ptr, double w_i,
                                const double* F0, const double* F1, const double* F2,
                                const double* __restrict__ U_cv, double* __restrict__ U_new, double* ext_old,
-                               double* ext_new, int write_ext, const double* __restrict__ gphi) {
-  FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext, gphi);
+                               double* ext_new, int write_ext, const double* __restrict__ gphi,
+                               const double* __restrict__ Ueq, const double* __restrict__ Weq) {
+  FvCandidate<D>::run(hw_blk(), g, fg, dt_ptr, w_i, F0, F1, F2, U_cv, U_new, ext_old, ext_new, write_ext, gphi, Ueq,
+                      Weq);
 }
 
 // W_cv (subcell layout) from the active region of an extended primitive
@@ -427,7 +449,7 @@ struct Troubles {
 static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double min_rho, double max_rho, double min_P,
                                            const unsigned char* __restrict__ mask,
                                            const double* __restrict__ ext_new, double* __restrict__ theta_src,
-                                           double* __restrict__ troubles) {
+                                           double* __restrict__ troubles, const double* __restrict__ Weq) {
   constexpr int P_ = D + 1;
   const long long q = B.id * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nq) return;
@@ -438,8 +460,13 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double 
   const int pt0 = m & 1u, ptP = (m >> P_) & 1u;
   double t = (pt0 > ptP) ? (double)pt0 : (double)ptP;
   if (pad) {
-    const double r = ext_new[e];
-    const double P = ext_new[(long long)P_ * g.Nqe + e];
+    double r = ext_new[e];
+    double P = ext_new[(long long)P_ * g.Nqe + e];
+    if (Weq) {
+      // the full state's primitives (src/trouble_detection.py:59-60)
+      r = r + Weq[q];
+      P = P + Weq[(long long)P_ * g.Nq + q];
+    }
     t = (r >= min_rho) ? t : 1.0;
     t = (r <= max_rho) ? t : 1.0;
     t = (P >= min_P) ? t : 1.0;
@@ -451,8 +478,9 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double 
 template <int D>
 __global__ void k_troubles(Geo g, int pad, double min_rho, double max_rho, double min_P,
                            const unsigned char* __restrict__ mask, const double* __restrict__ ext_new,
-                           double* __restrict__ theta_src, double* __restrict__ troubles) {
-  Troubles<D>::run(hw_blk(), g, pad, min_rho, max_rho, min_P, mask, ext_new, theta_src, troubles);
+                           double* __restrict__ theta_src, double* __restrict__ troubles,
+                           const double* __restrict__ Weq) {
+  Troubles<D>::run(hw_blk(), g, pad, min_rho, max_rho, min_P, mask, ext_new, theta_src, troubles, Weq);
 }
 
 // extended-grid coordinates
@@ -679,16 +707,18 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
                                            const long long* __restrict__ list,
                                            const unsigned long long* __restrict__ count,
                                            const double* __restrict__ W_ext, double* __restrict__ Mpred,
-                                           double* __restrict__ S, unsigned char* ltape) {
+                                           double* __restrict__ S, unsigned char* ltape,
+                                           const double* __restrict__ Meq, const double* __restrict__ gphi) {
   constexpr int V = D + 2, P_ = D + 1;
   const unsigned long long cnt = *count;
   const double dti = *dt_ptr * w_i;
+  const bool wb = Meq != nullptr;
   for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
        idx += (unsigned long long)B.n * blockDim.x) {
   const long long e = list[idx];
   int c[3];
   e_coords(g, e, c[0], c[1], c[2]);
-  double W[V], dMh[3][V];
+  double W[V], dMh[3][V], dMq[3][V];
 #pragma unroll
   for (int v = 0; v < V; ++v) W[v] = W_ext[(long long)v * g.Nqe + e];
 #pragma unroll
@@ -707,8 +737,20 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
       else dm = limiter_br<BM>(limiter, SL, SR, hl, hr, hm, &ltape[((long long)d * V + v) * g.Nqe + e]);
       dMh[d][v] = dm;
       S[((long long)d * V + v) * g.Nqe + e] = 0.5 * dm * hm;
+      if (wb) {
+        // the equilibrium's limited gradient (src/muscl.py:203-204)
+        const double* Q = Meq + (long long)v * g.Nqe;
+        const double QL = div_rcp(Q[e] - Q[e - st], hl, rhl);
+        const double QR = div_rcp(Q[e + st] - Q[e], hr, rhr);
+        dMq[d][v] = (limiter == LIM_MINMOD) ? minmod(QL, QR) : moncen(QL, QR, hl, hr, hm);
+      }
     }
   }
+  // the prediction takes the full state in the well-balanced mode
+  // (src/muscl.py:205-207); the state it is added to is (M + M_eq) - M_eq
+  double Wf[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) Wf[v] = wb ? W[v] + Meq[(long long)v * g.Nqe + e] : W[v];
   double dtW[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) dtW[v] = 0.0;
@@ -716,15 +758,38 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
   for (int d = 0; d < D; ++d) {
     const int vel = d + 1;
     const double* dW = dMh[d];
-    dtW[0] = dtW[0] - (W[vel] * dW[0] + W[0] * dW[vel]);
-    dtW[P_] = dtW[P_] - (W[vel] * dW[P_] + g.gamma * W[P_] * dW[vel]);
-    dtW[vel] = dtW[vel] - (W[vel] * dW[vel] + dW[P_] / W[0]);
+    dtW[0] = dtW[0] - (Wf[vel] * dW[0] + Wf[0] * dW[vel]);
+    dtW[P_] = dtW[P_] - (Wf[vel] * dW[P_] + g.gamma * Wf[P_] * dW[vel]);
+    dtW[vel] = dtW[vel] - (Wf[vel] * dW[vel] + dW[P_] / Wf[0]);
+    if (wb) {
+      // src/muscl.py:167-170; the transverse terms then use the
+      // equilibrium gradient, as the reference's reassigned dW does
+      dW = dMq[d];
+      dtW[0] = dtW[0] - (Wf[vel] * dW[0]);
+      dtW[P_] = dtW[P_] - (Wf[vel] * dW[P_]);
+    }
 #pragma unroll
-    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - W[vel] * dW[v2];
+    for (int v2 = 2; v2 <= D; ++v2) dtW[v2] = dtW[v2] - Wf[vel] * dW[v2];
   }
   dtW[P_] = dtW[P_] * 0.0;
+  if (wb && gphi != nullptr) {
+    // gravity in the prediction (src/muscl.py:208-212), active subcells only
+    bool active = true;
 #pragma unroll
-  for (int v = 0; v < V; ++v) Mpred[(long long)v * g.Nqe + e] = W[v] + 0.5 * dtW[v] * dti;
+    for (int d = 0; d < D; ++d) active = active && c[d] >= NGH && c[d] < NGH + g.X[d];
+    if (active) {
+      const double drho = (Wf[0] - Meq[e]) / Wf[0];
+      const long long q = (c[0] - NGH) + (long long)g.X[0] * ((D > 1 ? c[1] - NGH : 0) +
+                                                            (long long)g.X[1] * (D > 2 ? c[2] - NGH : 0));
+#pragma unroll
+      for (int d = 0; d < D; ++d) dtW[d + 1] = dtW[d + 1] + drho * gphi[(long long)d * g.Nq + q];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const double base = wb ? Wf[v] - Meq[(long long)v * g.Nqe + e] : W[v];
+    Mpred[(long long)v * g.Nqe + e] = base + 0.5 * dtW[v] * dti;
+  }
   }
 }
 };
@@ -732,8 +797,8 @@ template <int D, int BM = 0>
 __global__ void k_muscl_cells(Geo g, FvGeo fg, int limiter, const double* __restrict__ dt_ptr, double w_i,
                               const long long* __restrict__ list, const unsigned long long* __restrict__ count,
                               const double* __restrict__ W_ext, double* __restrict__ Mpred, double* __restrict__ S,
-                              unsigned char* ltape = nullptr) {
-  MusclCells<D, BM>::run(hw_blk(), g, fg, limiter, dt_ptr, w_i, list, count, W_ext, Mpred, S, ltape);
+                              unsigned char* ltape, const double* __restrict__ Meq, const double* __restrict__ gphi) {
+  MusclCells<D, BM>::run(hw_blk(), g, fg, limiter, dt_ptr, w_i, list, count, W_ext, Mpred, S, ltape, Meq, gphi);
 }
 
 // fallback Riemann flux on the affected faces of direction d
@@ -746,15 +811,21 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d, int solve
                                            const long long* __restrict__ flist,
                                            const unsigned long long* __restrict__ fcount,
                                            const double* __restrict__ Mpred, const double* __restrict__ S,
-                                           double* __restrict__ F_FB, unsigned* ftape) {
+                                           double* __restrict__ F_FB, unsigned* ftape,
+                                           const double* __restrict__ Mq, const double* __restrict__ Fq) {
   const unsigned long long cnt = *fcount;
   for (unsigned long long idx = B.id * (unsigned long long)blockDim.x + threadIdx.x; idx < cnt;
        idx += (unsigned long long)B.n * blockDim.x)
-    face(g, d, solver, flist[idx], Mpred, S, F_FB, ftape);
+    face(g, d, solver, flist[idx], Mpred, S, F_FB, ftape, Mq, Fq);
 }
+// Mq, Fq (well-balanced mode): the equilibrium's primitive state and flux
+// at the faces, added to both states and subtracted from the flux
+// (src/fv_simulator.py:150-165)
 static __device__ __forceinline__ void face(const Geo& g, int d, int solver, long long fidx,
                                             const double* __restrict__ Mpred, const double* __restrict__ S,
-                                            double* __restrict__ F_FB, unsigned* ftape) {
+                                            double* __restrict__ F_FB, unsigned* ftape,
+                                            const double* __restrict__ Mq = nullptr,
+                                            const double* __restrict__ Fq = nullptr) {
   constexpr int V = D + 2;
   const long long nf = n_faces(g, d);
   const int FX = g.X[0] + (d == 0), FY = g.X[1] + (d == 1);
@@ -773,20 +844,25 @@ static __device__ __forceinline__ void face(const Geo& g, int d, int solver, lon
   for (int v = 0; v < V; ++v) {
     ML[v] = Mpred[(long long)v * g.Nqe + i1] + S[((long long)d * V + v) * g.Nqe + i1];
     MR[v] = Mpred[(long long)v * g.Nqe + i2] - S[((long long)d * V + v) * g.Nqe + i2];
+    if (Mq) {
+      MR[v] = MR[v] + Mq[(long long)v * nf + fidx];
+      ML[v] = ML[v] + Mq[(long long)v * nf + fidx];
+    }
   }
   Br<BM> br;
   if (BM == 2) br.w = ftape[fidx];
   riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, true, &br, g.iso != 0);
   if (BM == 1) ftape[fidx] = br.w;
 #pragma unroll
-  for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = F[v];
+  for (int v = 0; v < V; ++v) F_FB[(long long)v * nf + fidx] = Fq ? F[v] - Fq[(long long)v * nf + fidx] : F[v];
 }
 };
 template <int D, int BM = 0>
 __global__ void k_muscl_faces(Geo g, int d, int solver, const long long* __restrict__ flist,
                               const unsigned long long* __restrict__ fcount, const double* __restrict__ Mpred,
-                              const double* __restrict__ S, double* __restrict__ F_FB, unsigned* ftape = nullptr) {
-  MusclFaces<D, BM>::run(hw_blk(), g, d, solver, flist, fcount, Mpred, S, F_FB, ftape);
+                              const double* __restrict__ S, double* __restrict__ F_FB, unsigned* ftape,
+                              const double* __restrict__ Mq, const double* __restrict__ Fq) {
+  MusclFaces<D, BM>::run(hw_blk(), g, d, solver, flist, fcount, Mpred, S, F_FB, ftape, Mq, Fq);
 }
 
 // corrected update of the subcells next to an affected face
@@ -799,7 +875,8 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
                                            const double* F1, const double* F2, const double* B0, const double* B1,
                                            const double* B2, const double* A0, const double* A1, const double* A2,
                                            const double* __restrict__ U_cv, double* __restrict__ U_new,
-                                           double* __restrict__ ext_new, const double* __restrict__ gphi) {
+                                           double* __restrict__ ext_new, const double* __restrict__ gphi,
+                                           const double* __restrict__ Ueq, const double* __restrict__ Weq) {
   constexpr int V = D + 2;
   const unsigned long long cnt = *count;
   const double* FH[3] = {F0, F1, F2};
@@ -847,7 +924,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const FvGeo& fg,
     // (k_fv_candidate with write_ext == 2) or, after the last substep, W_cv
     // (k_ext_to_plain)
     double W[V];
-    prim<D>(un, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+    prims_cv<D>(g, un, W, Ueq, Weq, q);
     const long long e = ext_of<D>(g, ix, iy, iz);
 #pragma unroll
     for (int v = 0; v < V; ++v) ext_new[(long long)v * g.Nqe + e] = W[v];
@@ -861,9 +938,48 @@ __global__ void k_fv_correct(Geo g, FvGeo fg, const double* __restrict__ dt_ptr,
                              const double* F0, const double* F1, const double* F2, const double* B0,
                              const double* B1, const double* B2, const double* A0, const double* A1,
                              const double* A2, const double* __restrict__ U_cv, double* __restrict__ U_new,
-                             double* __restrict__ ext_new, const double* __restrict__ gphi) {
+                             double* __restrict__ ext_new, const double* __restrict__ gphi,
+                             const double* __restrict__ Ueq, const double* __restrict__ Weq) {
   FvCorrect<D>::run(hw_blk(), g, fg, dt_ptr, w_i, godunov, list, count, F0, F1, F2, B0, B1, B2, A0, A1, A2, U_cv,
-                    U_new, ext_new, gphi);
+                    U_new, ext_new, gphi, Ueq, Weq);
+}
+
+// Well-balanced mode around the step (src/sdader_simulator.py:363-376):
+// sign -1: U_sp -= U_eq_sp before the predictor; sign +1: U_sp += U_eq_sp
+// after the update.  One thread per solution-point value.
+struct WbShift {
+  static __device__ __forceinline__ void run(Blk B, long long n, double sign, double* __restrict__ U_sp,
+                                             const double* __restrict__ Ueq) {
+    const long long i = B.id * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    U_sp[i] = (sign < 0.0) ? U_sp[i] - Ueq[i] : U_sp[i] + Ueq[i];
+  }
+};
+static __global__ void k_wb_shift(long long n, double sign, double* __restrict__ U_sp, const double* __restrict__ Ueq) {
+  WbShift::run(hw_blk(), n, sign, U_sp, Ueq);
+}
+// U_cv += U_eq_cv, then W_cv = prim(U_cv) (src/sdader_simulator.py:375-376)
+template <int D>
+struct WbEnd {
+  static __device__ __forceinline__ void run(Blk B, const Geo& g, double* __restrict__ U_cv,
+                                             const double* __restrict__ Ueq, double* __restrict__ W_cv) {
+    constexpr int V = D + 2;
+    const long long q = B.id * (long long)blockDim.x + threadIdx.x;
+    if (q >= g.Nq) return;
+    double u[V], W[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      u[v] = U_cv[(long long)v * g.Nq + q] + Ueq[(long long)v * g.Nq + q];
+      U_cv[(long long)v * g.Nq + q] = u[v];
+    }
+    prim<D>(u, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) W_cv[(long long)v * g.Nq + q] = W[v];
+  }
+};
+template <int D>
+__global__ void k_wb_end(Geo g, double* __restrict__ U_cv, const double* __restrict__ Ueq, double* __restrict__ W_cv) {
+  WbEnd<D>::run(hw_blk(), g, U_cv, Ueq, W_cv);
 }
 
 // dt = cfl * h / cmax from the reduced maximum of d*c_s + sum |v| (NaN when

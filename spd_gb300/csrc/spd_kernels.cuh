@@ -145,7 +145,8 @@ template <int D, int P, int BM = 0, int DIR = -1>
 struct RiemannSd {
 static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Teff, int solver,
                                            const double* __restrict__ trace, const double* __restrict__ bcfix,
-                                           double* __restrict__ Fi, unsigned* tape) {
+                                           double* __restrict__ Fi, unsigned* tape,
+                                           const double* __restrict__ meq) {
   using k = K<D, P>;
   const int d = (DIR >= 0) ? DIR : d_rt;
   const long long nI = n_iface(g, d);
@@ -184,8 +185,12 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   const long long ct = (d == 0) ? (cy + (long long)g.N[1] * cz) : (d == 1 ? (cx + (long long)g.N[0] * cz)
                                                                             : (cx + (long long)g.N[0] * cy));
   const long long ntrans = g.Nc / Nd;
+  // the edge state: the trace of the iterate, plus (well-balanced mode,
+  // src/sdader_simulator.py:221-223) the equilibrium at that flux point
   auto tr = [&](int side, int v, long long cell) -> double {
-    return trace[(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
+    double val = trace[(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
+    if (meq) val = val + meq[(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
+    return val;
   };
   auto fix = [&](int side, int v) -> double {
     return bcfix[(((long long)side * k::V + v) * k::NJ + j) * ntrans + ct];
@@ -236,8 +241,9 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
 };
 template <int D, int P, int BM = 0, int DIR = -1>
 __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
-                             const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape = nullptr) {
-  RiemannSd<D, P, BM, DIR>::run(hw_blk(), g, d_rt, Teff, solver, trace, bcfix, Fi, tape);
+                             const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape,
+                             const double* __restrict__ meq) {
+  RiemannSd<D, P, BM, DIR>::run(hw_blk(), g, d_rt, Teff, solver, trace, bcfix, Fi, tape, meq);
 }
 
 // ---------------------------------------------------------------------------
@@ -266,11 +272,14 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
                                            const double* Fi1, const double* Fi2, double* tr0, double* tr1,
                                            double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
                                            const double* G0 = nullptr, const double* G1 = nullptr,
-                                           const double* G2 = nullptr, const double* gphi = nullptr) {
+                                           const double* G2 = nullptr, const double* gphi = nullptr,
+                                           const double* const* meqs = nullptr,
+                                           const double* const* feqs = nullptr) {
   using k = K<D, P>;
   const double* Gv[3] = {G0, G1, G2};
   const bool visc = EXT && G0 != nullptr;
   const bool pot = EXT && gphi != nullptr;
+  const bool wb = EXT && meqs != nullptr;
   extern __shared__ double dudt_s[];  // [(v*NS + s)*Teff + tl][CPB]
   const int CPB = blockDim.x;
   const int cl = threadIdx.x, tl = threadIdx.y;
@@ -301,6 +310,11 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
           double M[k::V], W[k::V], F[k::V];
 #pragma unroll
           for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
+          if (wb) {
+#pragma unroll
+            for (int v = 0; v < k::V; ++v)
+              M[v] = M[v] + meqs[d][((((long long)v * k::NJ + j) * k::nf + f)) * g.Nc + c];
+          }
           prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
           flux<D>(W, F, g.gamma, d, g.iso != 0);
 #pragma unroll
@@ -310,6 +324,14 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
         for (int v = 0; v < k::V; ++v) {
           Fl[v][0] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + il];
           Fl[v][k::nf - 1] = Fi[d][(((long long)v * g.T + tl) * k::NJ + j) * nI + ir];
+        }
+        if (wb) {
+          // F -> F' (src/sdader_simulator.py:235-237), before the viscous flux
+#pragma unroll
+          for (int v = 0; v < k::V; ++v)
+#pragma unroll
+            for (int f = 0; f < k::nf; ++f)
+              Fl[v][f] = Fl[v][f] - feqs[d][(((long long)v * k::NJ + j) * k::nf + f) * g.Nc + c];
         }
         if (visc) {
 #pragma unroll
@@ -407,9 +429,13 @@ struct InteriorExt {
                                              const double* Fi0, const double* Fi1, const double* Fi2, double* tr0,
                                              double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
                                              const double* G0, const double* G1, const double* G2,
-                                             const double* gphi) {
+                                             const double* gphi, const double* M0, const double* M1,
+                                             const double* M2, const double* E0, const double* E1,
+                                             const double* E2) {
+    const double* meqs[3] = {M0, M1, M2};
+    const double* feqs[3] = {E0, E1, E2};
     Interior<D, P, true>::run(B, op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2, Ffp0,
-                              Ffp1, Ffp2, G0, G1, G2, gphi);
+                              Ffp1, Ffp2, G0, G1, G2, gphi, M0 ? meqs : nullptr, feqs);
   }
 };
 template <int D, int P>
@@ -417,9 +443,11 @@ __global__ void k_interior_ext(Ops op, Geo g, int mode, int Teff, const double* 
                                const double* __restrict__ dt_ptr, double* __restrict__ U_sp,
                                double* __restrict__ U_ader, const double* Fi0, const double* Fi1, const double* Fi2,
                                double* tr0, double* tr1, double* tr2, double* Ffp0, double* Ffp1, double* Ffp2,
-                               const double* G0, const double* G1, const double* G2, const double* gphi) {
+                               const double* G0, const double* G1, const double* G2, const double* gphi,
+                               const double* M0, const double* M1, const double* M2, const double* E0,
+                               const double* E1, const double* E2) {
   InteriorExt<D, P>::run(hw_blk(), op, g, mode, Teff, Uin, Tu, dt_ptr, U_sp, U_ader, Fi0, Fi1, Fi2, tr0, tr1, tr2,
-                         Ffp0, Ffp1, Ffp2, G0, G1, G2, gphi);
+                         Ffp0, Ffp1, Ffp2, G0, G1, G2, gphi, M0, M1, M2, E0, E1, E2);
 }
 
 // ---------------------------------------------------------------------------

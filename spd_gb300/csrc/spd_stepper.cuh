@@ -104,21 +104,24 @@ struct Stepper : StepperBase {
             unsigned* no_tape = nullptr;
             if (d == 0)
               launch<RiemannSd<D, P, 0, 0>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, 0>, nb, 128, 0, g, d, Teff,
-                                            solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
+                                            solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
+                                            (const double*)C->Meq_fp[d]);
             else if (d == 1)
               launch<RiemannSd<D, P, 0, D1>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D1>, nb, 128, 0, g, d, Teff,
-                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
+                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
+                                            (const double*)C->Meq_fp[d]);
             else
               launch<RiemannSd<D, P, 0, D2>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D2>, nb, 128, 0, g, d, Teff,
-                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape);
+                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
+                                            (const double*)C->Meq_fp[d]);
           } else {
             unsigned* tp = C->tape_rs[d] + ((size_t)C->tape_step * C->T + it) * C->T * k::NJ * n_iface(g, d);
             if (C->tape_mode == 1)
               k_riemann_sd<D, P, 1><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                 C->bcfix[d], C->Fi[d], tp);
+                                                                                 C->bcfix[d], C->Fi[d], tp, nullptr);
             else
               k_riemann_sd<D, P, 2><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                 C->bcfix[d], C->Fi[d], tp);
+                                                                                 C->bcfix[d], C->Fi[d], tp, nullptr);
           }
         }
         CKL();
@@ -133,7 +136,8 @@ struct Stepper : StepperBase {
           ProfScope ps_(C, "k_visc_grad");
           launch<ViscGrad<D, P>>(C, "k_visc_grad", k_visc_grad<D, P>, blocks_for(g.Nc * Teff, 128), 128, 0, C->ops,
                                  g, Teff, Uin, Tu, C->trace[0], C->trace[1], C->trace[2], C->bcfix[0], C->bcfix[1],
-                                 C->bcfix[2], C->Wfp[0], C->Wfp[1], C->Wfp[2], C->dWsp);
+                                 C->bcfix[2], C->Wfp[0], C->Wfp[1], C->Wfp[2], C->dWsp, (const double*)C->Meq_fp[0],
+                                 (const double*)C->Meq_fp[1], (const double*)C->Meq_fp[2]);
         }
         CKL();
         {
@@ -150,12 +154,15 @@ struct Stepper : StepperBase {
       const int rows = (mode == 0 && Teff == 1 && cpb % 32 == 0) ? C->T : Teff;
       dim3 block(cpb, rows);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
-      if (visc || C->gphi_sp) {
+      if (visc || C->gphi_sp || C->Ueq_sp) {
         ProfScope ps_(C, "k_interior");
         launch<InteriorExt<D, P>>(C, "k_interior", k_interior_ext<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops,
                                   g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2],
                                   C->trace[0], C->trace[1], C->trace[2], C->Ffp[0], C->Ffp[1], C->Ffp[2],
-                                  visc ? C->Gv[0] : nullptr, C->Gv[1], C->Gv[2], (const double*)C->gphi_sp);
+                                  visc ? C->Gv[0] : nullptr, C->Gv[1], C->Gv[2], (const double*)C->gphi_sp,
+                                  (const double*)C->Meq_fp[0], (const double*)C->Meq_fp[1],
+                                  (const double*)C->Meq_fp[2], (const double*)C->Feq_fp[0],
+                                  (const double*)C->Feq_fp[1], (const double*)C->Feq_fp[2]);
       } else {
         ProfScope ps_(C, "k_interior");
         launch<Interior<D, P>>(C, "k_interior", k_interior<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops, g, mode,
@@ -248,7 +255,8 @@ struct Stepper : StepperBase {
         ProfScope ps_(C, "k_fv_candidate");
         launch<FvCandidate<D>>(C, "k_fv_candidate", k_fv_candidate<D>, blocks_for(g.Nq, BS), BS, 0, g, C->fvg, C->dt,
                                w_i, FH[0], FH[1], FH[2], C->U_cv, C->U_new, C->ext_old, C->ext_new,
-                               cf.FB ? (i == 0 ? 1 : 2) : 0, (const double*)C->gphi_fv);
+                               cf.FB ? (i == 0 ? 1 : 2) : 0, (const double*)C->gphi_fv, (const double*)C->Ueq_cv,
+                               (const double*)C->Weq_cv);
       }
       CKL();
       if (cf.FB && C->tape_mode == 2) {
@@ -290,7 +298,8 @@ struct Stepper : StepperBase {
         {
           ProfScope ps_(C, "k_troubles");
           launch<Troubles<D>>(C, "k_troubles", k_troubles<D>, blocks_for(g.Nq, BS), BS, 0, g, cf.PAD, cf.min_rho,
-                              cf.max_rho, cf.min_P, C->mask, C->ext_new, C->theta_src, C->troubles);
+                              cf.max_rho, cf.min_P, C->mask, C->ext_new, C->theta_src, C->troubles,
+                              (const double*)C->Weq_cv);
         }
         CKL();
         for (int d = 0; d < D; ++d) {
@@ -371,15 +380,16 @@ struct Stepper : StepperBase {
             if (C->tape_mode == 0) {
               unsigned* no_tape = nullptr;
               launch<MusclFaces<D>>(C, "k_muscl_faces", k_muscl_faces<D>, nb, BS, 0, g, d, cf.riemann_solver_fv,
-                                    C->list_face[d], fcount, C->Mpred, C->S, C->F_FB[d], no_tape);
+                                    C->list_face[d], fcount, C->Mpred, C->S, C->F_FB[d], no_tape,
+                                    (const double*)C->Meq_faces[d], (const double*)C->Feq_faces[d]);
             } else {
               unsigned* tp = C->tape_fb[d] + ((size_t)C->tape_step * C->T + i) * nface[d];
               if (C->tape_mode == 1)
                 k_muscl_faces<D, 1><<<nb, BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, C->list_face[d], fcount,
-                                                             C->Mpred, C->S, C->F_FB[d], tp);
+                                                             C->Mpred, C->S, C->F_FB[d], tp, nullptr, nullptr);
               else
                 k_muscl_faces<D, 2><<<nb, BS, 0, C->stream>>>(g, d, cf.riemann_solver_fv, C->list_face[d], fcount,
-                                                             C->Mpred, C->S, C->F_FB[d], tp);
+                                                             C->Mpred, C->S, C->F_FB[d], tp, nullptr, nullptr);
             }
           }
           CKL();
@@ -417,16 +427,18 @@ struct Stepper : StepperBase {
       unsigned char* no_tape = nullptr;
       launch<MusclCells<D>>(C, "k_muscl_cells", k_muscl_cells<D>, (unsigned)nb, 128, 0, g, C->fvg,
                             C->cfg.slope_limiter, C->dt, w_i, C->list_cell, C->counts, C->ext_old, C->Mpred, C->S,
-                            no_tape);
+                            no_tape, (const double*)C->Meq_fv, (const double*)C->gphi_fv);
       return;
     }
     unsigned char* lt = C->tape_lim + ((size_t)C->tape_step * C->T + i) * D * k::V * g.Nqe;
     if (C->tape_mode == 1)
       k_muscl_cells<D, 1><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i,
-                                                               C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt);
+                                                               C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt,
+                                                               nullptr, nullptr);
     else
       k_muscl_cells<D, 2><<<(unsigned)nb, 128, 0, C->stream>>>(g, C->fvg, C->cfg.slope_limiter, C->dt, w_i,
-                                                               C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt);
+                                                               C->list_cell, C->counts, C->ext_old, C->Mpred, C->S, lt,
+                                                               nullptr, nullptr);
   }
 
   // ext_new non-null: also the primitives of the corrected subcells (the
@@ -439,7 +451,7 @@ struct Stepper : StepperBase {
       launch<FvCorrect<D>>(C, "k_fv_correct", k_fv_correct<D>, (unsigned)nb, 128, 0, g, C->fvg, C->dt, w_i,
                            C->cfg.godunov, C->list_q, C->counts + 1, FH[0], FH[1], FH[2], C->F_FB[0], C->F_FB[1],
                            C->F_FB[2], C->aff[0], C->aff[1], C->aff[2], C->U_cv, C->U_new, ext_new,
-                           (const double*)C->gphi_fv);
+                           (const double*)C->gphi_fv, (const double*)C->Ueq_cv, (const double*)C->Weq_cv);
     }
   }
 
@@ -461,8 +473,49 @@ struct Stepper : StepperBase {
   // translation units)
   int vjp(spd_ctx* C) override { return adjoint_vjp<D, P>(C); }
 
+  // well-balanced mode: U_sp -/+ U_eq_sp around the step
+  int wb_shift(spd_ctx* C, double sign) {
+    const Geo& g = C->geo;
+    const long long n = (long long)k::V * k::NS * g.Nc;
+    {
+      ProfScope ps_(C, "k_wb_shift");
+      launch<WbShift>(C, "k_wb_shift", k_wb_shift, blocks_for(n, BS), BS, 0, n, sign, C->U_sp,
+                      (const double*)C->Ueq_sp);
+    }
+    CKL();
+    return 0;
+  }
+
+  int eq_prims(spd_ctx* C) override {
+    const Geo& g = C->geo;
+    {
+      ProfScope ps_(C, "k_prim_only");
+      launch<PrimOnly<D>>(C, "k_prim_only", k_prim_only<D>, blocks_for(g.Nq, BS), BS, 0, g, C->Ueq_cv, C->Weq_cv);
+    }
+    CKL();
+    return 0;
+  }
+
   int update(spd_ctx* C) override {
     const int final_mode = (C->cfg.update == SPD_UPDATE_SD) ? 1 : 2;
+    if (C->Ueq_sp) {
+      // src/sdader_simulator.py:363-365, 372-376: the step advances the
+      // perturbation; afterwards U_sp += U_eq_sp, U_cv += U_eq_cv (with the
+      // SD update U_cv is the previous step's) and W_cv = prim(U_cv)
+      if (int r = wb_shift(C, -1.0)) return r;
+      if (int r = predictor(C, final_mode)) return r;
+      if (C->cfg.update == SPD_UPDATE_FV)
+        if (int r = fv_update(C)) return r;
+      if (int r = wb_shift(C, 1.0)) return r;
+      const Geo& g = C->geo;
+      {
+        ProfScope ps_(C, "k_wb_end");
+        launch<WbEnd<D>>(C, "k_wb_end", k_wb_end<D>, blocks_for(g.Nq, BS), BS, 0, g, C->U_cv,
+                         (const double*)C->Ueq_cv, C->W_cv);
+      }
+      CKL();
+      return 0;
+    }
     if (int r = predictor(C, final_mode)) return r;
     if (C->cfg.update == SPD_UPDATE_FV) {
       if (int r = fv_update(C)) return r;

@@ -34,8 +34,12 @@ struct ViscGrad {
                                              const double* __restrict__ Uin, int Tu, const double* tr0,
                                              const double* tr1, const double* tr2, const double* bf0,
                                              const double* bf1, const double* bf2, double* W0, double* W1,
-                                             double* W2, double* __restrict__ dWsp) {
+                                             double* W2, double* __restrict__ dWsp, const double* mq0,
+                                             const double* mq1, const double* mq2) {
     using k = K<D, P>;
+    // well-balanced mode: the conservative equilibrium at the flux points is
+    // part of the state whose primitives are taken (src/sdader_simulator.py:221-223)
+    const double* meq[3] = {mq0, mq1, mq2};
     const long long tid = B.id * (long long)blockDim.x + threadIdx.x;
     if (tid >= g.Nc * Teff) return;
     const long long c = tid % g.Nc;
@@ -57,7 +61,9 @@ struct ViscGrad {
                                                                               : (cx + (long long)g.N[0] * cy));
       for (int j = 0; j < k::NJ; ++j) {
         auto tr = [&](int side, int v, long long cell) -> double {
-          return trace[d][(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
+          double val = trace[d][(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
+          if (meq[0]) val = val + meq[d][(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
+          return val;
         };
         auto fix = [&](int side, int v) -> double {
           return bcfix[d][(((long long)side * k::V + v) * k::NJ + j) * ntrans + ct];
@@ -73,7 +79,10 @@ struct ViscGrad {
         for (int f = 1; f < k::nf - 1; ++f) {
           double M[k::V], W[k::V];
 #pragma unroll
-          for (int v = 0; v < k::V; ++v) M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
+          for (int v = 0; v < k::V; ++v) {
+            M[v] = dot_dir<k::n>(op.sp_to_fp + f * k::n, u[v], d);
+            if (meq[0]) M[v] = M[v] + meq[d][(((long long)v * k::NJ + j) * k::nf + f) * g.Nc + c];
+          }
           prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
 #pragma unroll
           for (int v = 0; v < k::V; ++v) Wf[v][f] = W[v];
@@ -135,8 +144,9 @@ struct ViscGrad {
 template <int D, int P>
 __global__ void k_visc_grad(Ops op, Geo g, int Teff, const double* __restrict__ Uin, int Tu, const double* tr0,
                             const double* tr1, const double* tr2, const double* bf0, const double* bf1,
-                            const double* bf2, double* W0, double* W1, double* W2, double* __restrict__ dWsp) {
-  ViscGrad<D, P>::run(hw_blk(), op, g, Teff, Uin, Tu, tr0, tr1, tr2, bf0, bf1, bf2, W0, W1, W2, dWsp);
+                            const double* bf2, double* W0, double* W1, double* W2, double* __restrict__ dWsp,
+                            const double* mq0, const double* mq1, const double* mq2) {
+  ViscGrad<D, P>::run(hw_blk(), op, g, Teff, Uin, Tu, tr0, tr1, tr2, bf0, bf1, bf2, W0, W1, W2, dWsp, mq0, mq1, mq2);
 }
 
 template <int D, int P>

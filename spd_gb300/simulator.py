@@ -43,6 +43,30 @@ def _primitives(U, vels, _p_, gamma, isothermal=False):
     return W
 
 
+def _fluxes(W, vels, _p_, gamma, isothermal=False):
+    """src/hydro.py:127-170 on the host (setup of the well-balanced mode):
+    the Euler flux in the rotated frame ``vels``."""
+    F = W.copy()
+    v1 = vels[0]
+    K = W[0].copy() * 0
+    m = None
+    for v in vels[::-1]:
+        m = W[0] * W[v]
+        K += m * W[v]
+        F[v, ...] = m * W[v1]
+    E = W[_p_] / (gamma - 1) + 0.5 * K
+    F[0, ...] = m
+    F[v1, ...] = m * W[v1] + W[_p_]
+    F[_p_, ...] = W[v1] * (E + W[_p_])
+    F[_p_, ...] *= 0 if isothermal else 1
+    return F
+
+
+def _crop_fv(start, end, idim, ndim, ngh):
+    """src/slicing.py:27-31."""
+    return (Ellipsis,) + (slice(ngh, -ngh),) * (ndim - 1 - idim) + (slice(start, end),) + (slice(ngh, -ngh),) * idim
+
+
 def _conservatives(W, vels, _p_, gamma, isothermal=False):
     """src/hydro.py:88-125 on the host (setup and user-facing helper)."""
     U = W.copy()
@@ -329,16 +353,13 @@ class SD_Simulator(Simulator):
     GPU.  Constructed on its own it steps with the SD update and no
     limiter; SDADER_Simulator (its subclass) adds the options of the
     reference's SDADER class.  Options the GPU step does not implement
-    (WB, predictor=False, and viscosity with the FV update and FB, which
-    fails in the reference itself) raise NotImplementedError here, before
-    any device work.
+    (predictor=False, and viscosity with the FV update and FB, which fails
+    in the reference itself) raise NotImplementedError here, before any
+    device work.
     """
 
     def __init__(self, riemann_solver_sd: str = "llf", update: str = "SD", *args, **kwargs):
         super().__init__(*args, **kwargs)
-        for flag, name in ((self.WB, "WB"),):
-            if flag:
-                raise NotImplementedError(f"{name}=True is not implemented on the GPU path")
         # options of the classes below SD_Simulator in the reference's chain
         # (FV_Simulator, SDADER_Simulator), at their defaults when absent
         for key, val in (("riemann_solver_fv_name", "llf"), ("slope_limiter_name", "minmod"), ("predictor", True),
@@ -356,16 +377,16 @@ class SD_Simulator(Simulator):
             raise AttributeError(riemann_solver_sd)
         if update not in _lib.UPDATE:
             raise ValueError(f"update must be 'SD' or 'FV', got {update!r}")
-        if update == "FV" and self.FB and any(side == "eq" for d in self.dims for side in self.BC[d]):
+        if update == "FV" and self.FB and not self.WB and any(side == "eq" for d in self.dims for side in self.BC[d]):
             # src/fv_simulator.py:251-253 fills "eq" ghost subcells with zeros
             # (the perturbation of the well-balanced mode, not implemented
             # here); the reference's MUSCL-Hancock fluxes at those faces are
             # then NaN, and theta*F_FB + (1-theta)*F_HO turns the boundary
             # cells into NaN in the first step and every cell in the second
             raise NotImplementedError(
-                "BC 'eq' with update='FV' and FB=True: the reference's fallback fluxes at those boundaries are "
-                "NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes NaN in the "
-                "first two steps; this combination is refused instead of reproducing a NaN state")
+                "BC 'eq' with update='FV', FB=True and WB=False: the reference's fallback fluxes at those "
+                "boundaries are NaN (zero-density ghost subcells outside well-balanced mode), so its state becomes "
+                "NaN in the first two steps; this combination is refused instead of reproducing a NaN state")
         if self.viscosity and update == "FV" and self.FB:
             # src/fv_simulator.py:186-187 -> src/muscl.py:253 -> src/fv_simulator.py:74
             # -> src/muscl.py:97 calls Slope_limiter.compute_gradient, which does
@@ -412,7 +433,63 @@ class SD_Simulator(Simulator):
         self._init_boundaries(U_sp, W_gh)
         if self.potential:
             self.init_potential()
+        if self.WB:
+            self.init_equilibrium_state()
         self.compute_dt()
+
+    def init_equilibrium_state(self) -> None:
+        """The equilibrium of the well-balanced mode, eq_fct(xyz, case)
+        (src/sdader_simulator.py:436-481), on the host as in the reference:
+        cell means with one ghost element layer, the solution-point and
+        conservative values, the flux-point values of every direction with
+        each element's left edge set to its left neighbour's right edge, their
+        fluxes and, with the FV update, the primitive states and fluxes at the
+        subcell faces and the primitives on the extended subcell grid.
+        Uploaded to the device (``upload_equilibrium``)."""
+        p, n, ndim = self.p, self.p + 1, self.ndim
+        W_gh = self.array_sp(ngh=self.Nghe)
+        for var in range(self.nvar):
+            W_gh[var] = quadrature_mean(self.mesh_cv, self.eq_fct, ndim, var)
+        W_sp = self.compute_sp_from_cv(W_gh)
+        U_sp = self.compute_conservatives(W_sp)
+        eq = {"U_eq_sp": self.crop(U_sp)}
+        eq["U_eq_cv"] = self.compute_cv_from_sp(eq["U_eq_sp"])
+        for dim in self.dims:
+            idim = self.dims[dim]
+            vels = np.roll(self.vels, -idim)
+            U = self.compute_fp_from_sp(U_sp, dim)
+            M_fp = self.crop(U)  # a view: the matching below also changes U
+            # elements 1.. along dim take their left edge from the element
+            # before (element axis idim+ndim places from the end)
+            inner = (slice(None),) * (idim + ndim)
+            edge0 = (Ellipsis, 0) + (slice(None),) * idim
+            edge1 = (Ellipsis, -1) + (slice(None),) * idim
+            M_fp[(Ellipsis, slice(1, None)) + inner][edge0] = M_fp[(Ellipsis, slice(None, -1)) + inner][edge1]
+            W = self.compute_primitives(U)
+            F = _fluxes(W, vels, self._p_, self.gamma, self.isothermal)
+            eq[f"M_eq_fp_{dim}"] = M_fp.copy()
+            eq[f"F_eq_fp_{dim}"] = self.crop(F).copy()
+            if self.update == "FV":
+                last = (Ellipsis, slice(None, -1)) + (slice(None),) * idim
+                W_faces = self.integrate_faces(W, dim, ader=False)[last]
+                W_faces = self.transpose_to_fv(W_faces)[_crop_fv(p + 1, -p, idim, ndim, p + 1)]
+                eq[f"M_eq_faces_{dim}"] = W_faces
+                eq[f"F_eq_faces_{dim}"] = _fluxes(W_faces, vels, self._p_, self.gamma, self.isothermal)
+        if self.update == "FV":
+            ngh = self.Nghc
+            M = self.transpose_to_fv(W_gh)
+            eq["M_eq_fv"] = M[_crop_fv(n - ngh, -(n - ngh), 0, ndim, n - ngh)] if n > ngh else M
+        self.upload_equilibrium(eq)
+
+    def upload_equilibrium(self, eq: dict) -> None:
+        """The well-balanced mode's equilibrium arrays (the reference's
+        dm.U_eq_sp, U_eq_cv, M_eq_fp_<d>, F_eq_fp_<d>, M_eq_faces_<d>,
+        F_eq_faces_<d>, M_eq_fv, in its layouts) to the device; they are
+        also kept in ``dm``."""
+        for name, arr in eq.items():
+            arr = np.ascontiguousarray(arr, dtype=np.float64)
+            setattr(self.dm, name, arr)
+            self._ctx.upload(name, arr)
 
     def init_potential(self) -> None:
         """Gradient of the gravity potential phi = init_fct(xyz, -1)
@@ -512,6 +589,7 @@ class SD_Simulator(Simulator):
         cfg.godunov = int(bool(self.godunov))
         cfg.potential = int(bool(self.potential))
         cfg.isothermal = int(bool(self.isothermal))
+        cfg.WB = int(bool(self.WB))
         cfg.viscosity = int(bool(self.viscosity))
         cfg.nu = float(self.nu)
         cfg.beta = float(self.beta)
@@ -764,7 +842,8 @@ class SD_Simulator(Simulator):
                     riemann_solver_fv=self.riemann_solver_fv_name, slope_limiter=self.slope_limiter_name,
                     BC=[list(self.BC[d]) for d in self.dims], gamma=self.gamma, cfl_coeff=self.cfl_coeff,
                     lims=[list(self.lim[d]) for d in self.dims], viscosity=bool(self.viscosity), nu=self.nu,
-                    beta=self.beta, potential=bool(self.potential), isothermal=bool(self.isothermal))
+                    beta=self.beta, potential=bool(self.potential), isothermal=bool(self.isothermal),
+                    WB=bool(self.WB))
 
     def save_state(self, path) -> None:
         """Write U_sp, U_cv, W_cv, the FV boundary buffers, time, n_step, dt

@@ -107,6 +107,40 @@ CASES = {
                                          riemann_solver_fv="llf", isothermal=True, potential=True,
                                          BC=(("periodic", "periodic"), ("reflective", "reflective"))),
                                     ("gravity_column", {"amp": 0.3, "step": True}), 3),
+    # well-balanced mode (src/sdader_simulator.py:436-481 and its uses):
+    # ``eq_ic`` is the equilibrium state's initial condition (eq_fct)
+    "wb_column8_p2_fvfb_hllc_eq": (dict(p=2, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                        riemann_solver_fv="hllc", WB=True, potential=True,
+                                        eq_ic=["gravity_column", {"amp": 0.0}],
+                                        BC=(("periodic", "periodic"), ("eq", "eq"))),
+                                   ("gravity_column", {"amp": 0.05, "step": True}), 5),
+    "wb_column8_p3_sd_hllc_reflective": (dict(p=3, N=(8, 8), update="SD", riemann_solver_sd="hllc", WB=True,
+                                              potential=True, eq_ic=["gravity_column", {"amp": 0.0}],
+                                              BC=(("periodic", "periodic"), ("reflective", "reflective"))),
+                                         ("gravity_column", {"amp": 0.05}), 5),
+    "wb_column8_p2_fv_llf_eq": (dict(p=2, N=(8, 8), update="FV", riemann_solver_sd="llf", WB=True,
+                                     potential=True, eq_ic=["gravity_column", {"amp": 0.0}],
+                                     BC=(("periodic", "periodic"), ("eq", "eq"))),
+                                ("gravity_column", {"amp": 0.05}), 4),
+    "wb_sine8_p3_fvfb_moncen_periodic": (dict(p=3, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                              riemann_solver_fv="llf", slope_limiter="moncen", WB=True,
+                                              eq_ic=["sine_wave", {}], BC=(("periodic", "periodic"),) * 2),
+                                         ("step_function", {}), 4),
+    "wb_column4_p2_fvfb_hllc_3d": (dict(p=2, N=(4, 3, 4), update="FV", FB=True, riemann_solver_sd="hllc",
+                                        riemann_solver_fv="hllc", WB=True, potential=True,
+                                        eq_ic=["gravity_column", {"amp": 0.0, "g": 1.5}],
+                                        BC=(("periodic", "periodic"), ("periodic", "periodic"), ("eq", "eq"))),
+                                   ("gravity_column", {"amp": 0.05, "g": 1.5, "step": True}), 3),
+    "wb_visc_column8_p2_sd_llf": (dict(p=2, N=(8, 8), update="SD", riemann_solver_sd="llf", WB=True,
+                                       potential=True, viscosity=True, nu=1e-3,
+                                       eq_ic=["gravity_column", {"amp": 0.0}],
+                                       BC=(("periodic", "periodic"), ("eq", "eq"))),
+                                  ("gravity_column", {"amp": 0.05}), 3),
+    "wb_iso_column8_p2_fvfb_hllc": (dict(p=2, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                         riemann_solver_fv="hllc", WB=True, potential=True, isothermal=True,
+                                         eq_ic=["gravity_column", {"amp": 0.0}],
+                                         BC=(("periodic", "periodic"), ("reflective", "reflective"))),
+                                    ("gravity_column", {"amp": 0.05, "step": True}), 3),
 }
 
 
@@ -141,10 +175,42 @@ LONG_CASES = {
     "visc_kh32_p3_sd_hllc_periodic_100steps": (dict(p=3, N=(32, 32), update="SD", riemann_solver_sd="hllc",
                                                     viscosity=True, nu=1e-3, BC=(("periodic", "periodic"),) * 2),
                                                ("kelvin_helmholtz", {"N": 32}), {"steps": 100}),
+    "wb_column16_p3_fvfb_hllc_eq_100steps": (dict(p=3, N=(16, 16), update="FV", FB=True, riemann_solver_sd="hllc",
+                                                  riemann_solver_fv="hllc", WB=True, potential=True,
+                                                  eq_ic=["gravity_column", {"amp": 0.0}],
+                                                  BC=(("periodic", "periodic"), ("eq", "eq"))),
+                                             ("gravity_column", {"amp": 0.05, "step": True}), {"steps": 100}),
     "step16_p3_sd_hllc_periodic_100steps": (dict(p=3, N=(16, 16), update="SD", riemann_solver_sd="hllc",
                                                  BC=(("periodic", "periodic"),) * 2),
                                             ("step_function", {}), {"steps": 100}),
 }
+
+
+def ref_kwargs(kw):
+    """Constructor keywords of a case: ``eq_ic`` becomes the eq_fct callback."""
+    kw = dict(kw)
+    if "eq_ic" in kw:
+        kw["eq_fct"] = make_ic(tuple(kw.pop("eq_ic")))
+    return kw
+
+
+def eq_arrays(s):
+    """The equilibrium arrays of the well-balanced mode
+    (src/sdader_simulator.py:436-481), when it is on."""
+    out = {}
+    if not s.WB:
+        return out
+    out["U_eq_sp"] = s.dm.U_eq_sp.copy()
+    out["U_eq_cv"] = s.dm.U_eq_cv.copy()
+    for d in s.dims:
+        out[f"M_eq_fp_{d}"] = getattr(s.dm, f"M_eq_fp_{d}").copy()
+        out[f"F_eq_fp_{d}"] = getattr(s.dm, f"F_eq_fp_{d}").copy()
+        if s.update == "FV":
+            out[f"M_eq_faces_{d}"] = getattr(s.dm, f"M_eq_faces_{d}").copy()
+            out[f"F_eq_faces_{d}"] = getattr(s.dm, f"F_eq_faces_{d}").copy()
+    if s.update == "FV":
+        out["M_eq_fv"] = s.dm.M_eq_fv.copy()
+    return out
 
 
 def make_ic(spec):
@@ -184,7 +250,7 @@ def main(ref_root, only=None, long=False):
         if only and name not in only:
             continue
         init = make_ic(icspec)
-        s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **kw)
+        s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **ref_kwargs(kw))
         out = {
             "sp_to_fp": s.dm.sp_to_fp, "fp_to_sp": s.dm.fp_to_sp, "dfp_to_sp": s.dm.dfp_to_sp,
             "sp_to_cv": s.dm.sp_to_cv, "fp_to_cv": s.dm.fp_to_cv, "cv_to_sp": s.dm.cv_to_sp,
@@ -198,6 +264,7 @@ def main(ref_root, only=None, long=False):
         if s.potential:
             out["grad_phi_sp"] = s.dm.grad_phi_sp.copy()
             out["grad_phi_fv"] = s.dm.grad_phi_fv.copy()
+        out.update(eq_arrays(s))
         s.init_sim()
         dts = []
         for _ in range(steps):
@@ -236,7 +303,7 @@ def main_long(SDADER_Simulator, rpoly, only):
         if only and name not in only:
             continue
         init = make_ic(icspec)
-        s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **kw)
+        s = SDADER_Simulator(init_fct=init, use_cupy=False, verbose=False, **ref_kwargs(kw))
         out = {
             "sp_to_fp": s.dm.sp_to_fp, "fp_to_sp": s.dm.fp_to_sp, "dfp_to_sp": s.dm.dfp_to_sp,
             "sp_to_cv": s.dm.sp_to_cv, "fp_to_cv": s.dm.fp_to_cv, "cv_to_sp": s.dm.cv_to_sp,
@@ -247,6 +314,10 @@ def main_long(SDADER_Simulator, rpoly, only):
             out[f"init_BC_fp_{d}"] = getattr(s.dm, f"BC_fp_{d}").copy()
             if s.update == "FV":
                 out[f"init_BC_fv_{d}"] = getattr(s.dm, f"BC_fv_{d}").copy()
+        if s.potential:
+            out["grad_phi_sp"] = s.dm.grad_phi_sp.copy()
+            out["grad_phi_fv"] = s.dm.grad_phi_fv.copy()
+        out.update(eq_arrays(s))
         limited = s.update == "FV" and s.FB
         s.init_sim()
         dts, crcs, counts = [], [], []

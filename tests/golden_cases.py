@@ -13,6 +13,8 @@ DIMS = ("x", "y", "z")
 
 
 LONG = os.path.join(GOLDEN, "long")
+# equilibrium arrays of the well-balanced mode in a fixture
+WB_KEYS = ("U_eq_sp", "U_eq_cv", "M_eq_fp", "F_eq_fp", "M_eq_faces", "F_eq_faces", "M_eq_fv")
 
 
 def long_case_names():
@@ -53,6 +55,9 @@ def load(name, where=GOLDEN):
         if key in kw:
             kw[key] = tuple(kw[key])
     kw["BC"] = tuple(tuple(b) for b in kw["BC"])
+    if "eq_ic" in kw:
+        # the equilibrium of the well-balanced mode, as a callback
+        kw["eq_fct"] = make_ic(tuple(kw.pop("eq_ic")))
     return data, kw, meta
 
 
@@ -81,6 +86,10 @@ def oracle_from_golden(data, kw):
     if kw.get("potential", False):
         state["grad_phi_sp"] = data["grad_phi_sp"]
         state["grad_phi_fv"] = data["grad_phi_fv"]
+    for key in WB_KEYS:
+        for name in (key, *(f"{key}_{d}" for d in DIMS[:ndim])):
+            if name in data:
+                state[name] = data[name]
     for d in DIMS[:ndim]:
         state[f"BC_fp_{d}"] = data[f"init_BC_fp_{d}"]
         if f"init_BC_fv_{d}" in data:
@@ -95,7 +104,7 @@ def oracle_from_golden(data, kw):
         max_rho=kw.get("max_rho", 1e10), min_P=kw.get("min_P", 1e-10), godunov=kw.get("godunov", False),
         ops=ops, state=state, viscosity=kw.get("viscosity", False), nu=kw.get("nu", 1e-4),
         beta=kw.get("beta", 2.0 / 3), potential=kw.get("potential", False),
-        isothermal=kw.get("isothermal", False))
+        isothermal=kw.get("isothermal", False), WB=kw.get("WB", False))
 
 
 def golden_operators(data):

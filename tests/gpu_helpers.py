@@ -27,7 +27,19 @@ def product_from_golden(data, kw, meta):
     if kw.get("potential", False):
         s.dm.grad_phi_sp = data["grad_phi_sp"]
         s.dm.grad_phi_fv = data["grad_phi_fv"]
+    if kw.get("WB", False):
+        s.upload_equilibrium({name: data[name] for name in wb_fields(s) if name in data})
     return s
+
+
+def wb_fields(s):
+    """Names of the well-balanced mode's equilibrium arrays for ``s``."""
+    from golden_cases import WB_KEYS
+    names = []
+    for key in WB_KEYS:
+        names += [key] if key in ("U_eq_sp", "U_eq_cv", "M_eq_fv") else [f"{key}_{d}" for d in s.dims]
+    return [n for n in names if s.update == "FV" or not (n.startswith("M_eq_faces") or
+                                                          n.startswith("F_eq_faces") or n == "M_eq_fv")]
 
 
 def oracle_like(s, **override):
@@ -58,10 +70,13 @@ def oracle_like(s, **override):
               slope_limiter=s.slope_limiter_name, update=s.update, FB=s.FB, tolerance=s.tolerance, SED=s.SED,
               NAD=s.NAD, PAD=s.PAD, blending=s.blending, min_rho=s.min_rho, max_rho=s.max_rho, min_P=s.min_P,
               godunov=s.godunov, ops=s.ops, state=state, viscosity=s.viscosity, nu=s.nu, beta=s.beta,
-              potential=s.potential, isothermal=s.isothermal)
+              potential=s.potential, isothermal=s.isothermal, WB=s.WB)
     if s.potential:
         state["grad_phi_sp"] = s.dm.grad_phi_sp
         state["grad_phi_fv"] = s.dm.grad_phi_fv
+    if s.WB:
+        for name in wb_fields(s):
+            state[name] = getattr(s.dm, name)
     kw.update(override)
     return OracleSDADER(**kw)
 
