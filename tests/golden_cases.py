@@ -27,12 +27,13 @@ def case_names():
 
 
 def adjoint_case_names():
-    """The golden cases the adjoint covers: not viscosity, gravity or the
-    isothermal system (spd_adjoint_enable refuses those)."""
+    """The golden cases the adjoint covers: not viscosity, gravity, the
+    isothermal system or the well-balanced mode (spd_adjoint_enable refuses
+    those)."""
     out = []
     for name in case_names():
         kw = load(name)[1]
-        if not (kw.get("viscosity") or kw.get("potential") or kw.get("isothermal")):
+        if not (kw.get("viscosity") or kw.get("potential") or kw.get("isothermal") or kw.get("WB")):
             out.append(name)
     return out
 
