@@ -861,11 +861,11 @@ def adjoint_fd_check(s, U0, target, dts, g, ndirs, eps=1e-6, seed=2028):
 
 def adjoint_batch(args, make_batch, n, nsteps):
     """B seeded instances (own targets), each gradient on its own context and
-    stream, driven by one host thread per instance."""
-    import concurrent.futures
+    stream, driven by ``spd_gb300.adjoint.AdjointBatch`` (one host thread per
+    instance)."""
     import numpy as np
     import torch
-    from spd_gb300.adjoint import AdjointRunner
+    from spd_gb300.adjoint import AdjointBatch, AdjointRunner
     B = args.batch
     sims = [make_batch(i) for i in range(B)]
     U0s = [torch.tensor(sm.dm.U_sp, device="cuda") for sm in sims]
@@ -881,20 +881,17 @@ def adjoint_batch(args, make_batch, n, nsteps):
     # 16 concurrent instances keep 4 slots each (checkpoints every 4 steps)
     every = 4
 
-    def one(i):
-        r = AdjointRunner(sims[i], nsteps, checkpoint_every=every)
-        y = r.forward(U0s[i])
-        res = y[0] - targets[i]
+    def loss_grad(i, y):
         gy = torch.zeros_like(y)
-        gy[0] = 2.0 * res
-        g = r.backward(gy)
-        return float(torch.linalg.vector_norm(g[0]))
+        gy[0] = 2.0 * (y[0] - targets[i])
+        return gy
 
+    batch = AdjointBatch(sims, nsteps, checkpoint_every=every)
     t0 = time.perf_counter()
-    with concurrent.futures.ThreadPoolExecutor(max_workers=B) as ex:
-        norms = list(ex.map(one, range(B)))
+    _, grads = batch.gradients(U0s, loss_grad)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    norms = [float(torch.linalg.vector_norm(g[0])) for g in grads]
     for sm in sims:
         sm.close()
     return {"instances": B, "wall_s": wall, "gradients_per_s": B / wall, "checkpoint_every": every,

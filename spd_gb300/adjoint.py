@@ -27,7 +27,7 @@ import math
 
 import torch
 
-__all__ = ["SDADERSteps", "AdjointRunner", "run_steps"]
+__all__ = ["SDADERSteps", "AdjointRunner", "AdjointBatch", "run_steps"]
 
 
 def _sync(t: torch.Tensor):
@@ -138,3 +138,56 @@ def run_steps(sim, U0: torch.Tensor, nsteps: int, checkpoint_every: int | None =
               refresh: bool = True) -> torch.Tensor:
     """Differentiable ``nsteps`` steps of ``sim`` starting from ``U0``."""
     return SDADERSteps.apply(U0, AdjointRunner(sim, nsteps, checkpoint_every, dts, refresh))
+
+
+class AdjointBatch:
+    """Gradients of many independent simulators at once.
+
+    Each instance keeps its own context, CUDA stream and ``AdjointRunner``;
+    one host thread per instance issues its forward and backward passes, so
+    the instances' kernels overlap on the GPU while every call of the
+    library still waits only for its own stream.  Every instance's result
+    is the one its ``AdjointRunner`` gives alone (the same launches on the
+    same data, bit for bit)."""
+
+    def __init__(self, sims, nsteps: int, checkpoint_every: int | None = None, dts=None, refresh: bool = True,
+                 max_workers: int | None = None):
+        if not sims:
+            raise ValueError("AdjointBatch needs at least one simulator")
+        if len({id(s._ctx) for s in sims}) != len(sims):
+            raise ValueError("AdjointBatch: every instance needs its own simulator (context)")
+        per = [None] * len(sims) if dts is None else list(dts)
+        if len(per) != len(sims):
+            raise ValueError("dts: one list per instance")
+        self.runners = [AdjointRunner(s, nsteps, checkpoint_every, d, refresh) for s, d in zip(sims, per)]
+        self.max_workers = int(max_workers or len(sims))
+
+    def _map(self, fn, items):
+        import concurrent.futures
+        with concurrent.futures.ThreadPoolExecutor(max_workers=self.max_workers) as ex:
+            return list(ex.map(fn, range(len(self.runners)), items))
+
+    def forward(self, U0s):
+        """Final states of every instance (one tensor per instance)."""
+        if len(U0s) != len(self.runners):
+            raise ValueError("one initial state per instance")
+        return self._map(lambda i, U0: self.runners[i].forward(U0), U0s)
+
+    def backward(self, grads_out):
+        """Gradients with respect to every instance's initial state."""
+        if len(grads_out) != len(self.runners):
+            raise ValueError("one output gradient per instance")
+        return self._map(lambda i, g: self.runners[i].backward(g), grads_out)
+
+    def gradients(self, U0s, loss_grad):
+        """forward, ``loss_grad(i, y_i) -> dJ/dy_i`` and backward of every
+        instance in its own thread (no instance waits for another's
+        forward); returns (final states, gradients)."""
+        if len(U0s) != len(self.runners):
+            raise ValueError("one initial state per instance")
+
+        def one(i, U0):
+            y = self.runners[i].forward(U0)
+            return y, self.runners[i].backward(loss_grad(i, y))
+        out = self._map(one, U0s)
+        return [o[0] for o in out], [o[1] for o in out]

@@ -128,3 +128,33 @@ def test_fixed_dts_are_replayed():
     assert r.dts == dts[::-1]
     with pytest.raises(ValueError):
         AdjointRunner(sim, 3, dts=[0.1])
+
+
+def test_adjoint_batch_equals_each_instance_alone():
+    """AdjointBatch (one host thread per instance) gives every instance the
+    gradient its AdjointRunner gives alone."""
+    from spd_gb300.adjoint import AdjointBatch, AdjointRunner
+    rng = np.random.default_rng(6)
+    shape = (2, 2, 2)
+    n = 8
+    nsteps = 5
+    problems = []
+    for b in range(4):
+        mats = [np.eye(n) + 0.1 * rng.standard_normal((n, n)) for _ in range(nsteps)]
+        shifts = [rng.standard_normal(n) for _ in range(nsteps)]
+        dts = [1e-3 * (j + 1 + 10 * b) for j in range(nsteps)]
+        problems.append((mats, shifts, dts))
+    U0s = [torch.tensor(rng.standard_normal(shape)) for _ in problems]
+    ws = [torch.tensor(rng.standard_normal(shape)) for _ in problems]
+    batch = AdjointBatch([FakeSim(FakeCtx(*pr), shape) for pr in problems], nsteps, checkpoint_every=2)
+    ys, gs = batch.gradients(U0s, lambda i, y: ws[i])
+    for i, pr in enumerate(problems):
+        r = AdjointRunner(FakeSim(FakeCtx(*pr), shape), nsteps, checkpoint_every=2)
+        y = r.forward(U0s[i])
+        g = r.backward(ws[i])
+        assert torch.equal(ys[i], y) and torch.equal(gs[i], g)
+    with pytest.raises(ValueError):
+        batch.forward(U0s[:2])
+    sim = FakeSim(FakeCtx(*problems[0]), shape)
+    with pytest.raises(ValueError):
+        AdjointBatch([sim, sim], nsteps)
