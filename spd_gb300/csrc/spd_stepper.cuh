@@ -79,6 +79,26 @@ struct Stepper : StepperBase {
     return 0;
   }
 
+  // the Riemann problems of one Picard iteration with every branch taped
+  // (BM 1) or replayed (BM 2), one instantiation per direction as in the
+  // plain form.  The runtime-direction instantiation is not used: on
+  // sm_103a its LLF branch returned NaN for every flux in 2D (HLLC, 1D and
+  // the same device function called from a plain kernel were exact).
+  template <int BM>
+  void riemann_taped(spd_ctx* C, int d, unsigned nb, int Teff, int solver, unsigned* tp) {
+    const Geo& g = C->geo;
+    constexpr int D1 = (D > 1 ? 1 : 0), D2 = (D > 2 ? 2 : 0);
+    if (d == 0)
+      k_riemann_sd<D, P, BM, 0><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d], C->bcfix[d], C->Fi[d],
+                                                          tp, nullptr);
+    else if (d == 1)
+      k_riemann_sd<D, P, BM, D1><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d], C->bcfix[d], C->Fi[d],
+                                                           tp, nullptr);
+    else
+      k_riemann_sd<D, P, BM, D2><<<nb, 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d], C->bcfix[d], C->Fi[d],
+                                                           tp, nullptr);
+  }
+
   int predictor(spd_ctx* C, int final_mode) {
     const Geo& g = C->geo;
     if (C->recording)
@@ -117,11 +137,9 @@ struct Stepper : StepperBase {
           } else {
             unsigned* tp = C->tape_rs[d] + ((size_t)C->tape_step * C->T + it) * C->T * k::NJ * n_iface(g, d);
             if (C->tape_mode == 1)
-              k_riemann_sd<D, P, 1><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                 C->bcfix[d], C->Fi[d], tp, nullptr);
+              riemann_taped<1>(C, d, blocks_for(tot, 128), Teff, solver, tp);
             else
-              k_riemann_sd<D, P, 2><<<blocks_for(tot, 128), 128, 0, C->stream>>>(g, d, Teff, solver, C->trace[d],
-                                                                                 C->bcfix[d], C->Fi[d], tp, nullptr);
+              riemann_taped<2>(C, d, blocks_for(tot, 128), Teff, solver, tp);
           }
         }
         CKL();

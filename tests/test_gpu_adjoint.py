@@ -185,3 +185,34 @@ def test_batched_gradients_equal_single_instance_gradients():
         s.close()
         assert torch.equal(ys[i], y) and torch.equal(gs[i], g), i
         assert torch.isfinite(g).all()
+
+
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+@pytest.mark.parametrize("solver", ["llf", "hllc", "lhllc"])
+@pytest.mark.parametrize("update", ["SD", "FV"])
+def test_taped_step_equals_plain_step(ndim, solver, update):
+    """One step with every decision taped (spd_tape_step mode 1) and its
+    replay (mode 2) give the plain step's state bit for bit, for every
+    Riemann solver, 1D-3D, SD and FV (with limiting) updates."""
+    from spd_gb300 import SDADER_Simulator
+    from spd_gb300 import initial_conditions as ics
+    N = {1: (16,), 2: (8, 6), 3: (4, 3, 4)}[ndim]
+    s = SDADER_Simulator(p=2 if ndim == 3 else 3, N=N, init_fct=ics.sine_wave, riemann_solver_sd=solver,
+                         riemann_solver_fv=solver, update=update, FB=update == "FV", verbose=False)
+    ctx = s._ctx
+    shape = s._shape_of("U_sp")
+    U0 = generic_point(s.dm.U_sp, ndim, seed=3)
+    ctx.tape_enable(1)
+    ctx.upload("U_sp", U0)
+    dt = ctx.compute_dt()
+    ctx.set_dt(dt)
+    ctx.perform_update(0.0)
+    plain = ctx.download("U_sp", shape)
+    out = []
+    for mode in (1, 2):
+        ctx.upload("U_sp", U0)
+        ctx.tape_step(0, dt, mode)
+        out.append(ctx.download("U_sp", shape))
+    s.close()
+    assert np.isfinite(plain).all()
+    assert np.array_equal(out[0], plain) and np.array_equal(out[1], plain)
