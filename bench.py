@@ -316,6 +316,53 @@ def vortex_t1_error():
     return out
 
 
+def other_configs(args, steps=5):
+    """The other single-GPU configurations timed like the headline (compute_dt
+    + perform_update per step, launch by launch, CUDA events on the
+    library's stream after 3 warm-up steps) and through the graph driver
+    (perform_iterations: one captured step replayed): the vortex 32^2 (p=3,
+    FV with limiting, LLF) and the 3D Sedov blast 128^3 (p=2, FV with
+    limiting, HLLC), each with its own clock record."""
+    import torch
+    from spd_gb300 import SDADER_Simulator
+    out = {}
+    for name in ("vortex32", "sedov128"):
+        kw = workload_kwargs(name)
+        dof, cells = dof_of(kw)
+        s = SDADER_Simulator(verbose=False, fma=args.build == "fma", **kw)
+        stream = torch.cuda.current_stream()
+        s._ctx.set_stream(stream.cuda_stream)
+        for _ in range(3):
+            s.compute_dt()
+            s.perform_update()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            for _ in range(steps):
+                s.compute_dt()
+                s.perform_update()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        s.time, _, _ = s._ctx.step(1, 0.0, 0, s.time)  # graph capture (untimed)
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        s.time, _, _ = s._ctx.step(steps, 0.0, 0, s.time)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gms = g0.elapsed_time(g1)
+        s.close()
+        out[name] = {"workload": WORKLOADS[name], "cells": cells, "dof": dof, "steps": steps, "warmup": 3,
+                     "ms_per_step": ms / steps, "value": dof * steps / (ms / 1e3), "unit": UNIT,
+                     "graph_driver": {"ms_per_step": gms / steps, "value": dof * steps / (gms / 1e3)},
+                     "clocks": clk.summary(),
+                     "l2": ("inputs smaller than L2 (launch-bound case)" if name == "vortex32"
+                            else "inputs larger than L2")}
+    return out
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -554,6 +601,7 @@ def ours(args):
                 "fp64_gemm_peak_tflops": fp64, "fp64_gemm_clocks": fp64_clocks,
                 "cpu_baseline": cpu, "parity_vs_oracle": parity,
                 "vortex_t1": vortex_t1_error() if world == 1 else None,
+                "other_configs": other_configs(args) if world == 1 and not args.cells else None,
                 "graph_driver": graph_driver,
                 "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks,
@@ -691,7 +739,8 @@ def ensemble_arm(args):
                 sm.perform_update()
 
     plain_loop(args.warmup)
-    plain_s = timed(lambda: plain_loop(args.steps))
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk_plain:
+        plain_s = timed(lambda: plain_loop(args.steps))
     ens, tuning = None, None
     if sims:
         if args.ensemble_form == "auto":
@@ -702,7 +751,8 @@ def ensemble_arm(args):
             tuning = {"form": args.ensemble_form, "streams": None if args.ensemble_form == "packed" else 16,
                       "cells_per_block": ens.cells_per_block()[0][0], "graph_nodes_per_step": ens.graph_nodes()}
         ens.perform_iterations(args.warmup)
-    batched_s = timed(lambda: ens.perform_iterations(args.steps) if ens else None)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk_batched:
+        batched_s = timed(lambda: ens.perform_iterations(args.steps) if ens else None)
     plain = dof * args.steps / plain_s
     batched = dof * args.steps / batched_s
     if rank == 0:
@@ -713,7 +763,9 @@ def ensemble_arm(args):
                 "config": {"workload": WORKLOADS[args.workload], "instances": len(sides), "sides": sides,
                            "dof_per_ensemble_step": dof,
                            "parallelism": f"instances sharded over {world} GPUs" if world > 1 else "1 GPU"},
-                "plain_loop_value": plain, "batched_over_plain": batched / plain, "autotune": tuning}
+                "plain_loop_value": plain, "plain_loop_ms_per_step": plain_s / args.steps * 1e3,
+                "batched_over_plain": batched / plain, "autotune": tuning,
+                "clocks": clk_batched.summary(), "plain_loop_clocks": clk_plain.summary()}
         print(json.dumps(line), flush=True)
     if ens:
         ens.close()
