@@ -373,6 +373,8 @@ class SD_Simulator(Simulator):
                                       "(the reference's path raises AttributeError)")
         if self.Nghc != 2:
             raise NotImplementedError("only Nghc=2 subcell ghost layers are supported")
+        if not 1 <= self.p <= 4:
+            raise NotImplementedError(f"p={self.p}: the kernels are instantiated for degrees 1 to 4")
         if riemann_solver_sd not in _lib.RIEMANN:
             raise AttributeError(riemann_solver_sd)
         if update not in _lib.UPDATE:

@@ -72,7 +72,7 @@ def test_subcell_faces_mirror_ghosts():
 
 
 def test_unsupported_options_raise():
-    for kw in ({"viscosity": True, "update": "FV", "FB": True}, {"predictor": False}):
+    for kw in ({"viscosity": True, "update": "FV", "FB": True}, {"predictor": False}, {"p": 0}, {"p": 5}):
         with pytest.raises(NotImplementedError):
             SDADER_Simulator(N=(4,), **kw)
     with pytest.raises(AttributeError):
