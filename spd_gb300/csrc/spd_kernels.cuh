@@ -141,7 +141,7 @@ __global__ void k_traces_ader(Ops op, Geo g, const double* __restrict__ U, int T
 // ---------------------------------------------------------------------------
 // DIR >= 0 fixes the direction at compile time (the rotated velocity
 // indices become constants); DIR = -1 takes it from d_rt.
-template <int D, int P, int BM = 0, int DIR = -1>
+template <int D, int P, int BM = 0, int DIR = -1, bool EQ = false>
 struct RiemannSd {
 static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Teff, int solver,
                                            const double* __restrict__ trace, const double* __restrict__ bcfix,
@@ -189,7 +189,7 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   // src/sdader_simulator.py:221-223) the equilibrium at that flux point
   auto tr = [&](int side, int v, long long cell) -> double {
     double val = trace[(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
-    if (meq) val = val + meq[(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
+    if constexpr (EQ) val = val + meq[(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
     return val;
   };
   auto fix = [&](int side, int v) -> double {
@@ -239,11 +239,13 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   for (int v = 0; v < k::V; ++v) Fi[(((long long)v * g.T + t) * k::NJ + j) * nI + iface] = F[v];
 }
 };
-template <int D, int P, int BM = 0, int DIR = -1>
+// EQ: the well-balanced mode's form (meq, the equilibrium at the flux
+// points, added to every edge state); the plain form reads no meq
+template <int D, int P, int BM = 0, int DIR = -1, bool EQ = false>
 __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
                              const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape,
                              const double* __restrict__ meq) {
-  RiemannSd<D, P, BM, DIR>::run(hw_blk(), g, d_rt, Teff, solver, trace, bcfix, Fi, tape, meq);
+  RiemannSd<D, P, BM, DIR, EQ>::run(hw_blk(), g, d_rt, Teff, solver, trace, bcfix, Fi, tape, meq);
 }
 
 // ---------------------------------------------------------------------------

@@ -79,6 +79,25 @@ struct Stepper : StepperBase {
     return 0;
   }
 
+  // the Riemann problems of one Picard iteration, one instantiation per
+  // direction; EQ adds the well-balanced mode's equilibrium edge values
+  template <bool EQ>
+  void riemann_plain(spd_ctx* C, int d, unsigned nb, int Teff, int solver) {
+    const Geo& g = C->geo;
+    constexpr int D1 = (D > 1 ? 1 : 0), D2 = (D > 2 ? 2 : 0);
+    unsigned* no_tape = nullptr;
+    const double* meq = C->Meq_fp[d];
+    if (d == 0)
+      launch<RiemannSd<D, P, 0, 0, EQ>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, 0, EQ>, nb, 128, 0, g, d, Teff,
+                                        solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape, meq);
+    else if (d == 1)
+      launch<RiemannSd<D, P, 0, D1, EQ>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D1, EQ>, nb, 128, 0, g, d, Teff,
+                                         solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape, meq);
+    else
+      launch<RiemannSd<D, P, 0, D2, EQ>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D2, EQ>, nb, 128, 0, g, d, Teff,
+                                         solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape, meq);
+  }
+
   // the Riemann problems of one Picard iteration with every branch taped
   // (BM 1) or replayed (BM 2), one instantiation per direction as in the
   // plain form.  The runtime-direction instantiation is not used: on
@@ -120,20 +139,10 @@ struct Stepper : StepperBase {
           ProfScope ps_(C, "k_riemann_sd");
           if (C->tape_mode == 0) {
             const unsigned nb = blocks_for(tot, 128);
-            constexpr int D1 = (D > 1 ? 1 : 0), D2 = (D > 2 ? 2 : 0);
-            unsigned* no_tape = nullptr;
-            if (d == 0)
-              launch<RiemannSd<D, P, 0, 0>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, 0>, nb, 128, 0, g, d, Teff,
-                                            solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
-                                            (const double*)C->Meq_fp[d]);
-            else if (d == 1)
-              launch<RiemannSd<D, P, 0, D1>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D1>, nb, 128, 0, g, d, Teff,
-                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
-                                            (const double*)C->Meq_fp[d]);
+            if (C->Meq_fp[d])
+              riemann_plain<true>(C, d, nb, Teff, solver);
             else
-              launch<RiemannSd<D, P, 0, D2>>(C, "k_riemann_sd", k_riemann_sd<D, P, 0, D2>, nb, 128, 0, g, d, Teff,
-                                             solver, C->trace[d], C->bcfix[d], C->Fi[d], no_tape,
-                                            (const double*)C->Meq_fp[d]);
+              riemann_plain<false>(C, d, nb, Teff, solver);
           } else {
             unsigned* tp = C->tape_rs[d] + ((size_t)C->tape_step * C->T + it) * C->T * k::NJ * n_iface(g, d);
             if (C->tape_mode == 1)

@@ -50,3 +50,29 @@ def test_flux_point_arrays_absent_with_the_sd_update():
     with pytest.raises(AttributeError, match="update='FV'"):
         s.dm.F_ader_fp_x
     s.close()
+
+
+@pytest.mark.parametrize("p", [1, 3])
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+@pytest.mark.parametrize("n", [1, 6])
+def test_transforms_round_trip_and_direction_symmetry(p, ndim, n):
+    """What the reference's test/test_transforms.py checks, on SD_Simulator
+    built with the device context (including single-element grids): the
+    subcell and flux-point transforms invert each other to 1e-14, and the
+    x and y flux-point interpolations agree up to the transposition.  The
+    single-element grid then also steps, bitwise as the oracle."""
+    from spd_gb300 import SD_Simulator
+    s = SD_Simulator(p=p, N=(n,) * ndim, verbose=False)
+    W_cv = s.dm.W_cv
+    assert np.all(np.abs(s.compute_cv_from_sp(s.compute_sp_from_cv(W_cv)) - W_cv) < 1e-14)
+    W_sp = s.dm.W_sp
+    assert np.all(np.abs(s.compute_sp_from_fp(s.compute_fp_from_sp(W_sp, "x"), "x") - W_sp) < 1e-14)
+    if ndim == 2:
+        W_x = s.transpose_to_fv(s.compute_fp_from_sp(W_sp, "x"))
+        W_y = np.transpose(s.transpose_to_fv(s.compute_fp_from_sp(W_sp, "y")), (0, 2, 1))
+        assert np.all(np.abs(W_x - W_y) < 1e-14)
+    o = oracle_like(s)
+    dts = step_both(s, o, 2)
+    assert all(a == b for a, b in dts)
+    assert not compare(s, o)
+    s.close()
