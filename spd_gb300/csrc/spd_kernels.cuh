@@ -189,7 +189,9 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   // src/sdader_simulator.py:221-223) the equilibrium at that flux point
   auto tr = [&](int side, int v, long long cell) -> double {
     double val = trace[(((long long)(side * k::V + v) * g.T + t) * k::NJ + j) * g.Nc + cell];
-    if constexpr (EQ) val = val + meq[(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
+    if constexpr (EQ) {
+      if (meq) val = val + meq[(((long long)v * k::NJ + j) * k::nf + (side ? k::nf - 1 : 0)) * g.Nc + cell];
+    }
     return val;
   };
   auto fix = [&](int side, int v) -> double {
@@ -233,14 +235,17 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int d_rt, int Te
   double F[k::V];
   Br<BM> br;
   if (BM == 2) br.w = tape[tid];
-  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, false, &br, g.iso != 0);
+  // the isothermal system only in the EQ form: a runtime flag costs the
+  // plain form an FP64 multiply per flux (the compiler predicates it)
+  riemann<D, double, BM>(solver, ML, MR, F, g.gamma, g.min_c2, d, false, &br, EQ && g.iso != 0);
   if (BM == 1) tape[tid] = br.w;
 #pragma unroll
   for (int v = 0; v < k::V; ++v) Fi[(((long long)v * g.T + t) * k::NJ + j) * nI + iface] = F[v];
 }
 };
-// EQ: the well-balanced mode's form (meq, the equilibrium at the flux
-// points, added to every edge state); the plain form reads no meq
+// EQ: the form for the well-balanced mode (meq non-null: the equilibrium
+// at the flux points added to every edge state) and the isothermal system;
+// the plain form reads neither
 template <int D, int P, int BM = 0, int DIR = -1, bool EQ = false>
 __global__ void k_riemann_sd(Geo g, int d_rt, int Teff, int solver, const double* __restrict__ trace,
                              const double* __restrict__ bcfix, double* __restrict__ Fi, unsigned* tape,
@@ -282,6 +287,9 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
   const bool visc = EXT && G0 != nullptr;
   const bool pot = EXT && gphi != nullptr;
   const bool wb = EXT && meqs != nullptr;
+  // the isothermal system runs in the EXT form only (a runtime flag would
+  // cost the plain form a predicated FP64 multiply per flux point)
+  const bool iso = EXT && g.iso != 0;
   extern __shared__ double dudt_s[];  // [(v*NS + s)*Teff + tl][CPB]
   const int CPB = blockDim.x;
   const int cl = threadIdx.x, tl = threadIdx.y;
@@ -317,8 +325,8 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
             for (int v = 0; v < k::V; ++v)
               M[v] = M[v] + meqs[d][((((long long)v * k::NJ + j) * k::nf + f)) * g.Nc + c];
           }
-          prim<D>(M, W, g.gamma, 0, (double*)nullptr, g.iso != 0);
-          flux<D>(W, F, g.gamma, d, g.iso != 0);
+          prim<D>(M, W, g.gamma, 0, (double*)nullptr, iso);
+          flux<D>(W, F, g.gamma, d, iso);
 #pragma unroll
           for (int v = 0; v < k::V; ++v) Fl[v][f] = F[v];
         }
@@ -376,7 +384,7 @@ static __device__ __forceinline__ void run(Blk B, const Ops& op, const Geo& g, i
           const double uv = Uin[(((long long)(d + 1) * Tu + tu) * k::NS + s) * g.Nc + c];
           double* sv = &dudt_s[((((long long)(d + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
           *sv = *sv + u0 * gp;
-          if (!g.iso) {
+          if (!iso) {
             double* sp = &dudt_s[((((long long)(D + 1)) * k::NS + s) * Teff + tl) * CPB + cl];
             *sp = *sp + uv * gp;
           }

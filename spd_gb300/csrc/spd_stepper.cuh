@@ -80,7 +80,8 @@ struct Stepper : StepperBase {
   }
 
   // the Riemann problems of one Picard iteration, one instantiation per
-  // direction; EQ adds the well-balanced mode's equilibrium edge values
+  // direction; EQ: the form with the well-balanced mode's equilibrium edge
+  // values and the isothermal system
   template <bool EQ>
   void riemann_plain(spd_ctx* C, int d, unsigned nb, int Teff, int solver) {
     const Geo& g = C->geo;
@@ -139,7 +140,7 @@ struct Stepper : StepperBase {
           ProfScope ps_(C, "k_riemann_sd");
           if (C->tape_mode == 0) {
             const unsigned nb = blocks_for(tot, 128);
-            if (C->Meq_fp[d])
+            if (C->Meq_fp[d] || C->cfg.isothermal)
               riemann_plain<true>(C, d, nb, Teff, solver);
             else
               riemann_plain<false>(C, d, nb, Teff, solver);
@@ -181,7 +182,7 @@ struct Stepper : StepperBase {
       const int rows = (mode == 0 && Teff == 1 && cpb % 32 == 0) ? C->T : Teff;
       dim3 block(cpb, rows);
       const size_t sm = (mode == 2) ? 0 : (size_t)k::V * k::NS * Teff * cpb * sizeof(double);
-      if (visc || C->gphi_sp || C->Ueq_sp) {
+      if (visc || C->gphi_sp || C->Ueq_sp || C->cfg.isothermal) {
         ProfScope ps_(C, "k_interior");
         launch<InteriorExt<D, P>>(C, "k_interior", k_interior_ext<D, P>, blocks_for(g.Nc, cpb), block, sm, C->ops,
                                   g, mode, Teff, Uin, Tu, C->dt, C->U_sp, C->U_ader, C->Fi[0], C->Fi[1], C->Fi[2],

@@ -2,9 +2,20 @@
 the domain integral of the conserved variables, sum over subcells of
 U_cv times the subcell volume, is unchanged by the step up to round-off
 wherever no flux crosses the boundary.  Kelvin-Helmholtz 512^2 (p=3,
-periodic: mass, momenta and energy) and the Sedov blast 128^3 (p=2,
-reflective walls: mass and energy), both with the FV update and
-limiting, the workloads' full sizes."""
+periodic: mass, momenta and energy) with the SD update and with the FV
+update without limiting, and the Sedov blast 128^3 (p=2, reflective
+walls: mass and energy) with the FV update and limiting, the workloads'
+full sizes.
+
+The reference's FV update with limiting is not conservative across
+periodic boundaries once troubled cells reach them: theta is blended on
+the padded array, the blending of the outer ghost layer is truncated, and
+the two copies of a periodic boundary face can get different theta
+(0.25 on one side, 0 on the other), so the two cells beside it see
+different fluxes (src/trouble_detection.py:139-169 with
+src/fv_simulator.py:224-273).  The product reproduces that bit for bit; the
+periodic case with limiting is therefore not a conservation case.
+"""
 import numpy as np
 import pytest
 
@@ -26,24 +37,30 @@ def _totals(s):
     return per_cell.sum(axis=axes_cells) * vol, np.abs(per_cell).sum(axis=axes_cells) * vol
 
 
-@pytest.mark.parametrize("case", ["kh512", "sedov128"])
+@pytest.mark.parametrize("case", ["kh512_sd", "kh512_fv", "sedov128_fvfb"])
 def test_conserved_totals_at_full_size(case):
     from spd_gb300 import SDADER_Simulator
     from spd_gb300 import initial_conditions as ics
-    if case == "kh512":
-        kw = dict(p=3, N=(512, 512), init_fct=ics.kelvin_helmholtz(512, seed=7), BC=(("periodic", "periodic"),) * 2)
+    if case.startswith("kh512"):
+        kw = dict(p=3, N=(512, 512), init_fct=ics.kelvin_helmholtz(512, seed=7), BC=(("periodic", "periodic"),) * 2,
+                  update="SD" if case == "kh512_sd" else "FV", FB=False)
         conserved = [0, 1, 2, 3]
     else:
-        kw = dict(p=2, N=(128, 128, 128), init_fct=ics.sedov(128), BC=(("reflective", "reflective"),) * 3)
+        kw = dict(p=2, N=(128, 128, 128), init_fct=ics.sedov(128), BC=(("reflective", "reflective"),) * 3,
+                  update="FV", FB=True)
         conserved = [0, 4]
-    s = SDADER_Simulator(update="FV", FB=True, riemann_solver_sd="hllc", riemann_solver_fv="hllc", verbose=False,
-                         **kw)
+    s = SDADER_Simulator(riemann_solver_sd="hllc", riemann_solver_fv="hllc", verbose=False, **kw)
+    # the initial U_cv holds the conservatives of the primitive averages;
+    # the step's U_cv are the subcell averages of U_sp (end_sim's form)
+    s.init_sim()
+    s.end_sim()
     t0, a0 = _totals(s)
     s.perform_iterations(5)
     t1, _ = _totals(s)
-    troubles = float(s.dm.troubles.sum())
+    troubles = float(s.dm.troubles.sum()) if s.FB else None
     s.close()
     assert np.isfinite(t1).all()
-    assert troubles > 0  # the fallback (and its blending) is part of what is conserved
+    if s.FB:
+        assert troubles > 0  # the fallback (and its blending) is part of what is conserved
     for v in conserved:
         assert abs(t1[v] - t0[v]) <= 1e-12 * a0[v], (v, t0[v], t1[v])
