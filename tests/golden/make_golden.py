@@ -61,6 +61,26 @@ CASES = {
                                             riemann_solver_sd="hllc", riemann_solver_fv="llf",
                                             BC=(("gradfree", "reflective"), ("periodic", "periodic"))),
                                        ("four_quadrant", {}), 3),
+    # degree 4, time orders m != p, the fixed-state boundaries (ic,
+    # pressure), another gamma and CFL, PAD off, p=1 in 3D
+    "quadrant8_p4_fvfb_hllc_gradfree": (dict(p=4, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                             riemann_solver_fv="hllc", BC=(("gradfree", "gradfree"),) * 2),
+                                        ("four_quadrant", {}), 3),
+    "quadrant8_p3_m1_fvfb_ic_pressure": (dict(p=3, m=1, N=(8, 8), update="FV", FB=True, riemann_solver_sd="hllc",
+                                              riemann_solver_fv="hllc", BC=(("ic", "ic"), ("pressure", "pressure"))),
+                                         ("four_quadrant", {}), 3),
+    "sod24_p4_m2_sd_lhllc_ic": (dict(p=4, m=2, N=(24,), update="SD", riemann_solver_sd="lhllc",
+                                     BC=(("ic", "gradfree"),)), ("sod", {}), 5),
+    "vortex16_p2_m4_fv_llf_gamma53": (dict(p=2, m=4, N=(16, 16), xlim=(0, 10), ylim=(0, 10), update="FV", FB=False,
+                                           riemann_solver_sd="llf", gamma=5.0 / 3.0, cfl_coeff=0.5,
+                                           BC=(("periodic", "periodic"),) * 2), ("vortex", {}), 3),
+    "quadrant8_p3_fvfb_nopad_moncen_mixed": (dict(p=3, N=(8, 8), update="FV", FB=True, PAD=False,
+                                                  slope_limiter="moncen", riemann_solver_sd="lhllc",
+                                                  riemann_solver_fv="hllc",
+                                                  BC=(("reflective", "pressure"), ("ic", "gradfree"))),
+                                             ("four_quadrant", {}), 3),
+    "sine6_p1_fvfb_llf_3d": (dict(p=1, N=(6, 6, 6), update="FV", FB=True, riemann_solver_sd="llf",
+                                  riemann_solver_fv="llf", BC=(("periodic", "periodic"),) * 3), ("sine_wave", {}), 3),
     # viscosity (src/sdader_simulator.py:245-268): SD update and the FV
     # update without limiting (with FB=True the reference's viscous fallback
     # fluxes raise AttributeError, src/muscl.py:253, src/muscl.py:97)
