@@ -363,6 +363,60 @@ def other_configs(args, steps=5):
     return out
 
 
+FULL_RUNS = {
+    # workload: (what the configuration runs to, driver)
+    "quadrant512": ("t_end", 0.8),
+    "sedov128": ("steps", 200),
+    "vortex32": ("t_end", 1.0),
+    "vortex512_sd": ("steps", 200),
+    "quadrant512_lhllc_moncen": ("t_end", 0.8),
+}
+
+
+def full_run_arm(args):
+    """The workload's whole run as its configuration specifies it (the
+    four-quadrant problem to t=0.8, the Sedov blast for 200 steps, ...)
+    through the reference's drivers (perform_time_evolution /
+    perform_iterations: one captured step replayed per step), timed with
+    CUDA events: steps, time to solution, DOF-updates/s over the run, and
+    the state's health at the end (finite, trouble count)."""
+    import numpy as np
+    import torch
+    from spd_gb300 import SDADER_Simulator
+    kind, target = FULL_RUNS[args.workload]
+    kw = workload_kwargs(args.workload, args.cells)
+    dof, cells = dof_of(kw)
+    t_setup = time.perf_counter()
+    s = SDADER_Simulator(verbose=False, fma=args.build == "fma", **kw)
+    t_setup = time.perf_counter() - t_setup
+    stream = torch.cuda.current_stream()
+    s._ctx.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    import contextlib
+    # the drivers' end-of-run line (the reference prints it) goes to stderr:
+    # stdout carries the one JSON line
+    with ClockSampler(0) as clk, contextlib.redirect_stdout(sys.stderr):
+        e0.record(stream)
+        if kind == "t_end":
+            s.perform_time_evolution(target)
+        else:
+            s.perform_iterations(target)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    U = s.dm.U_sp
+    out = {"metric": METRIC + " over a whole run", "value": dof * s.n_step / (ms / 1e3), "unit": UNIT,
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic", "build": args.build,
+           "config": {"workload": WORKLOADS[args.workload], "cells": cells, "dof": dof, "run": {kind: target}},
+           "steps": s.n_step, "t_final": s.time, "time_to_solution_s": ms / 1e3, "ms_per_step": ms / s.n_step,
+           "setup_s": t_setup, "finite": bool(np.isfinite(U).all()),
+           "troubled_subcells_last_step": float(s.dm.troubles.sum()) if s.update == "FV" and s.FB else None,
+           "clocks": clk.summary()}
+    s.close()
+    print(json.dumps(out), flush=True)
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -973,6 +1027,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=200, help="time steps of the differentiated run (kh_adjoint)")
     ap.add_argument("--fd-dirs", type=int, default=0, help="central-difference directions to check (kh_adjoint)")
     ap.add_argument("--batch", type=int, default=1, help="seeded instances run concurrently (kh_adjoint)")
+    ap.add_argument("--full-run", action="store_true",
+                    help="the workload's whole run as its configuration specifies (t_end or step count) through "
+                         "perform_time_evolution / perform_iterations")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -989,6 +1046,10 @@ def main():
         from spd_gb300.build import build
         build()
         adjoint_arm(args)
+    elif args.full_run:
+        from spd_gb300.build import build
+        build()
+        full_run_arm(args)
     else:
         from spd_gb300.build import build
         if int(os.environ.get("LOCAL_RANK", "0")) == 0:

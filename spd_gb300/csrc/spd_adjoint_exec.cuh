@@ -172,12 +172,17 @@ int adjoint_vjp(spd_ctx* C) {
           }
         }
       }
-      {
-        ProfScope ps_(C, "k_adj_prim_cv");
-        k_adj_prim_cv<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, Ucv_i, C->Unew_a, C->W_a, C->Ucv_a);
+      if (cf.FB) {
+        {
+          ProfScope ps_(C, "k_adj_prim_cv");
+          k_adj_prim_cv<D><<<blocks_for(g.Nq, BS), BS, 0, C->stream>>>(g, Ucv_i, C->Unew_a, C->W_a, C->Ucv_a);
+        }
+        CKL();
+        std::swap(C->Ucv_a, C->Unew_a);  // the adjoint of this substep's input feeds the previous one
       }
-      CKL();
-      std::swap(C->Ucv_a, C->Unew_a);  // the adjoint of this substep's input feeds the previous one
+      // without limiting the substep's input enters only through the
+      // identity (its primitives feed no fallback flux): Unew_a already is
+      // the adjoint of the input, and W_a (allocated with FB only) is unused
     }
     {
       ProfScope ps_(C, "k_adj_sp_to_cv");

@@ -79,6 +79,8 @@ CASES = {
                                                   riemann_solver_fv="hllc",
                                                   BC=(("reflective", "pressure"), ("ic", "gradfree"))),
                                              ("four_quadrant", {}), 3),
+    "quadrant8_p2_fv_nofb_hllc_eq": (dict(p=2, N=(8, 8), update="FV", FB=False, riemann_solver_sd="hllc",
+                                          BC=(("eq", "gradfree"), ("periodic", "eq"))), ("four_quadrant", {}), 3),
     "sine6_p1_fvfb_llf_3d": (dict(p=1, N=(6, 6, 6), update="FV", FB=True, riemann_solver_sd="llf",
                                   riemann_solver_fv="llf", BC=(("periodic", "periodic"),) * 3), ("sine_wave", {}), 3),
     # viscosity (src/sdader_simulator.py:245-268): SD update and the FV
