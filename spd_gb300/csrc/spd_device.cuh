@@ -130,26 +130,57 @@ __device__ __noinline__ double div_ieee_slow(double a, double b) { return a / b;
 #else
 inline double div_ieee_slow(double a, double b) { return a / b; }
 #endif
-SPD_FN long long abs_bits_of(double x) {
+// Predicates on a double's bit pattern evaluated on its two 32-bit words
+// (integer pipes).  The same tests written on the 64-bit pattern (for
+// instance (bits & ~sign) > bits(inf) for NaN) were compiled to FP64-pipe
+// instructions, measured with ncu (one per test), on the pipe that bounds
+// the step's kernels.
+SPD_FN unsigned hi_word(double x) {
 #ifdef __CUDA_ARCH__
-  return __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return (unsigned)__double2hiint(x);
 #else
-  long long bits;
-  memcpy(&bits, &x, sizeof(bits));
-  return bits & 0x7fffffffffffffffLL;
+  unsigned long long b;
+  memcpy(&b, &x, sizeof(b));
+  return (unsigned)(b >> 32);
 #endif
 }
+SPD_FN unsigned lo_word(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned)__double2loint(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, sizeof(b));
+  return (unsigned)b;
+#endif
+}
+// x is a NaN
+SPD_FN bool nan_w(double x) {
+  const unsigned h = hi_word(x) & 0x7fffffffu;
+  return h > 0x7ff00000u || (h == 0x7ff00000u && lo_word(x) != 0u);
+}
+// x != 0 (true for NaN, false for both zeros)
+SPD_FN bool nonzero_w(double x) { return ((hi_word(x) & 0x7fffffffu) | lo_word(x)) != 0u; }
+// x > 0 (false for zeros, negatives and NaN)
+SPD_FN bool gt0_w(double x) {
+  const unsigned h = hi_word(x), l = lo_word(x);
+  return (h >> 31) == 0u && (h | l) != 0u && (h < 0x7ff00000u || (h == 0x7ff00000u && l == 0u));
+}
+
 SPD_FN double div_rcp(double a, double b, double rb) {
   const double q = a * rb;
   const double r = fma(-q, b, a);
   const double q2 = fma(r, rb, q);
-  constexpr long long INF = 0x7ff0000000000000LL;
-  const long long ea = abs_bits_of(a) >> 52, eb = abs_bits_of(b) >> 52, eq = abs_bits_of(q) >> 52;
-  const long long ab = abs_bits_of(a), bb = abs_bits_of(b);
-  if (eb >= 23 && eb <= 2023) {
-    if (ab == 0 || ab >= INF) return q;
-    if (ea >= 63 && ea <= 2023 && eq >= 63 && eq <= 2023) return q2;
-  } else if (bb == 0 || bb >= INF) {
+  // the window tests on the high words (|x|'s exponent is bits 30..20 of
+  // the high word; |x| is zero when both words of |x| are, infinite or NaN
+  // when the high word of |x| is >= that of infinity): integer pipes, where
+  // the same tests on the 64-bit patterns cost about one FP64 instruction
+  // per quotient (measured with ncu)
+  const unsigned ha = hi_word(a) & 0x7fffffffu, hb = hi_word(b) & 0x7fffffffu, hq = hi_word(q) & 0x7fffffffu;
+  const unsigned ea = ha >> 20, eb = hb >> 20, eq = hq >> 20;
+  if (eb >= 23u && eb <= 2023u) {
+    if ((ha | lo_word(a)) == 0u || ha >= 0x7ff00000u) return q;
+    if (ea >= 63u && ea <= 2023u && eq >= 63u && eq <= 2023u) return q2;
+  } else if ((hb | lo_word(b)) == 0u || hb >= 0x7ff00000u) {
     return q;
   }
   return div_ieee_slow(a, b);
@@ -169,7 +200,7 @@ SPD_FN Dual<N> ad_sqrt(const Dual<N>& x) {
 // |x| by clearing the sign bit (integer pipe; the same bits as fabs)
 SPD_FN double abs_bits(double x) {
 #ifdef __CUDA_ARCH__
-  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+  return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
 #else
   return fabs(x);
 #endif
@@ -198,24 +229,31 @@ template <class S>
 SPD_FN S np_max(const S& a, const S& b) { return (a >= b || a != a) ? a : b; }
 template <class S>
 SPD_FN S np_min(const S& a, const S& b) { return (a <= b || a != a) ? a : b; }
-// The same two functions for doubles on the device, evaluated on integer
-// keys that order the doubles as IEEE comparison does (-0 equal to +0,
-// NaN first): identical results, no FP64-pipe comparison.
-#ifdef __CUDA_ARCH__
-__device__ __forceinline__ long long ieee_key(long long b) {
-  b = (b == (long long)0x8000000000000000ULL) ? 0 : b;
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+// Order-preserving int64 key of a double's bit pattern b: negatives
+// reflected and moved up by one, so that -0 and +0 share the key 0 and every
+// other pair of non-NaN values compares as in IEEE (shifts, xor and a
+// subtraction on the integer pipes).
+SPD_FN long long ieee_key(long long b) {
+  const long long s = b >> 63;  // 0 or -1
+  return (b ^ (s & 0x7fffffffffffffffLL)) - s;
 }
-__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+// its inverse (the key 0 gives +0)
+SPD_FN long long ieee_key_inverse(long long k) {
+  const long long s = k >> 63;
+  return (k + s) ^ (s & 0x7fffffffffffffffLL);
+}
+// The same two functions for doubles on the device, evaluated on the
+// integer keys (NaN first): identical results, no FP64-pipe comparison.
+#ifdef __CUDA_ARCH__
 template <>
 __device__ __forceinline__ double np_max<double>(const double& a, const double& b) {
   const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
-  return (nan_bits(ba) || (!nan_bits(bb) && ieee_key(ba) >= ieee_key(bb))) ? a : b;
+  return (nan_w(a) || (!nan_w(b) && ieee_key(ba) >= ieee_key(bb))) ? a : b;
 }
 template <>
 __device__ __forceinline__ double np_min<double>(const double& a, const double& b) {
   const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
-  return (nan_bits(ba) || (!nan_bits(bb) && ieee_key(ba) <= ieee_key(bb))) ? a : b;
+  return (nan_w(a) || (!nan_w(b) && ieee_key(ba) <= ieee_key(bb))) ? a : b;
 }
 #endif
 // Dual forms: same value; at a tie the derivative is the mean of the two

@@ -45,20 +45,12 @@ __host__ __device__ __forceinline__ long long n_faces(const Geo& g, int d) {
   return (long long)(g.X[0] + (d == 0)) * (g.X[1] + (d == 1)) * (g.X[2] + (d == 2));
 }
 
-// Order-preserving int64 key of a double (ordering of the non-NaN values,
-// -0 mapped to +0 so that the two zeros compare equal as in IEEE) and its
-// inverse; NaN test on the bits.
-__device__ __forceinline__ long long order_key(double x) {
-  long long b = __double_as_longlong(x);
-  if (b == (long long)0x8000000000000000ULL) b = 0;
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-__device__ __forceinline__ double from_order_key(long long k) {
-  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
-}
-__device__ __forceinline__ bool is_nan_bits(double x) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-}
+// Order-preserving int64 key of a double (ieee_key of its bits: the two
+// zeros share a key, as they compare equal in IEEE) and its inverse (the
+// key of either zero gives +0); NaN test on the bits.
+__device__ __forceinline__ long long order_key(double x) { return ieee_key(__double_as_longlong(x)); }
+__device__ __forceinline__ double from_order_key(long long k) { return __longlong_as_double(ieee_key_inverse(k)); }
+__device__ __forceinline__ bool is_nan_bits(double x) { return nan_w(x); }
 // NumPy maximum (a if a >= b or a is NaN, else b) on the integer pipes
 __device__ __forceinline__ double np_max_key(double a, double b) {
   if (is_nan_bits(a)) return a;
@@ -66,14 +58,9 @@ __device__ __forceinline__ double np_max_key(double a, double b) {
   return order_key(a) >= order_key(b) ? a : b;
 }
 // x != 0.0 on the bits (true for NaN, false for both zeros)
-__device__ __forceinline__ bool nonzero_bits(double x) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) != 0;
-}
+__device__ __forceinline__ bool nonzero_bits(double x) { return nonzero_w(x); }
 // x > 0 on the bits (false for zeros, negatives and NaN)
-__device__ __forceinline__ bool gt0_key(double x) {
-  const long long b = __double_as_longlong(x);
-  return b > 0 && b <= 0x7ff0000000000000LL;
-}
+__device__ __forceinline__ bool gt0_key(double x) { return gt0_w(x); }
 
 // gravity source of one subcell (src/fv_simulator.py:200-203 with
 // src/simulator.py:197-203): dUdt[vel] += rho * dphi_vel, dUdt[P] +=

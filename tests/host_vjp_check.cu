@@ -163,9 +163,55 @@ double check_predictor(std::mt19937_64& rng) {
   return sqrt(err / nrm);
 }
 
+// ieee_key / ieee_key_inverse (the integer keys of the device max / min
+// and of the trouble detection) against IEEE comparison: every ordered
+// pair of non-NaN values, specials included, compares the same way on the
+// keys, and the inverse returns the value (+0 for either zero); and the
+// word-based predicates nan_w, nonzero_w, gt0_w against x != x, x != 0,
+// x > 0.
+long long check_order_keys(std::mt19937_64& rng, long long n) {
+  auto bits = [](double x) { long long b; memcpy(&b, &x, 8); return b; };
+  auto val = [](long long b) { double x; memcpy(&x, &b, 8); return x; };
+  const double specials[] = {0.0, -0.0, 1.0, -1.0, 4.9e-324, -4.9e-324, 2.2250738585072014e-308,
+                             -2.2250738585072014e-308, 1.7976931348623157e308, -1.7976931348623157e308,
+                             INFINITY, -INFINITY, 0.75, -0.25, 1e-300, -1e300};
+  std::uniform_int_distribution<unsigned long long> U;
+  long long bad = 0;
+  auto one = [&](double a, double b) {
+    if (a != a || b != b) return;
+    const long long ka = ieee_key(bits(a)), kb = ieee_key(bits(b));
+    bad += ((ka < kb) != (a < b)) + ((ka == kb) != (a == b)) + ((ka > kb) != (a > b));
+  };
+  auto preds = [&](double a) {
+    bad += (nan_w(a) != (a != a)) + (nonzero_w(a) != (a != 0.0)) + (gt0_w(a) != (a > 0.0));
+  };
+  for (double a : specials) {
+    preds(a);
+    for (double b : specials) one(a, b);
+  }
+  preds(NAN);
+  preds(-NAN);
+  preds(val(0x7ff0000000000001LL));
+  preds(val((long long)0xfff0000000000001ULL));
+  for (long long i = 0; i < n; ++i) {
+    const double a = val((long long)U(rng)), b = val((long long)U(rng));
+    one(a, b);
+    one(a, -a);
+    preds(a);
+    if (a == a) {
+      const double back = val(ieee_key_inverse(ieee_key(bits(a))));
+      bad += (a == 0.0) ? (bits(back) != 0) : (bits(back) != bits(a));
+    }
+  }
+  return bad;
+}
+
 int main() {
   std::mt19937_64 rng(42);
   double worst = 0.0;
+  const long long key_bad = check_order_keys(rng, 5000000);
+  printf("order-key mismatches: %lld\n", key_bad);
+  if (key_bad) return 1;
   const long long div_bad = check_div_rcp(rng, 20000000);
   printf("div_rcp mismatches: %lld of 20000000\n", div_bad);
   if (div_bad) return 1;
