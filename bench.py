@@ -200,7 +200,7 @@ def compulsory_bytes_per_cell_step(D, p):
 # one pass).  Keyed by (D, p, update, build).
 NCU_K_INTERIOR = {
     (2, 3, "FV", "ieee"): {"cells_captured": 256 * 256, "dram_bytes": 12085.9 + 14239.4, "fp64_inst": 42043.0},
-    (2, 3, "FV", "fma"): {"cells_captured": 256 * 256, "dram_bytes": 12134.0 + 14250.6, "fp64_inst": 29938.0},
+    (2, 3, "FV", "fma"): {"cells_captured": 256 * 256, "dram_bytes": 12122.4 + 14251.4, "fp64_inst": 28651.0},
 }
 
 

@@ -256,6 +256,20 @@ __device__ __forceinline__ double np_min<double>(const double& a, const double& 
   return (nan_w(a) || (!nan_w(b) && ieee_key(ba) <= ieee_key(bb))) ? a : b;
 }
 #endif
+// a > b with IEEE semantics (false when either is NaN; -0 equals +0).  For
+// doubles on the device it is evaluated on the integer keys: an FP64
+// comparison issues on the FP64 pipe, which bounds the Riemann solvers.
+SPD_FN bool fgt(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return !nan_w(a) && !nan_w(b) && ieee_key(__double_as_longlong(a)) > ieee_key(__double_as_longlong(b));
+#else
+  return a > b;
+#endif
+}
+template <int N> SPD_FN bool fgt(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
+template <int N> SPD_FN bool fgt(const Dual<N>& a, double b) { return a.v > b; }
+template <int N> SPD_FN bool fgt(double a, const Dual<N>& b) { return a > b.v; }
+
 // Dual forms: same value; at a tie the derivative is the mean of the two
 // arguments' derivatives (the subgradient torch.maximum / torch.minimum
 // propagate).
@@ -382,7 +396,7 @@ template <class S, int BM = 0>
 SPD_FN S sound_speed(const S& P, const S& rho, double gamma, double min_c2,
                                          Br<BM>* br = nullptr, const S* rrho = nullptr) {
   S c2 = rrho ? div_by(gamma * P, rho, *rrho) : gamma * P / rho;
-  c2 = pick(br, c2 > min_c2) ? c2 : S(min_c2);
+  c2 = pick(br, fgt(c2, min_c2)) ? c2 : S(min_c2);
   return ad_sqrt(c2);
 }
 
@@ -398,7 +412,7 @@ SPD_FN void llf(const S* WL, const S* WR, const S* UL, const S* UR, S* F, double
   flux<D>(WR, FR, gamma, idim, iso);
   const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
   const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br, rR) + abs_br(WR[v1], br);
-  const S cmax = pick(br, cL > cR) ? cL : cR;
+  const S cmax = pick(br, fgt(cL, cR)) ? cL : cR;
   const S hc = 0.5 * cmax;
 #pragma unroll
   for (int v = 0; v < V; ++v) F[v] = 0.5 * (FR[v] + FL[v]) - hc * (UR[v] - UL[v]);
@@ -414,10 +428,10 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
   const int v1 = rvel<D>(idim, 0);
   const S cL = sound_speed(WL[P_], WL[0], gamma, min_c2, br, rL) + abs_br(WL[v1], br);
   const S cR = sound_speed(WR[P_], WR[0], gamma, min_c2, br, rR) + abs_br(WR[v1], br);
-  const S cmax = pick(br, cL > cR) ? cL : cR;
+  const S cmax = pick(br, fgt(cL, cR)) ? cL : cR;
   const S vL = WL[v1], vR = WR[v1];
-  const S sL = (pick(br, vL < vR) ? vL : vR) - cmax;
-  const S sR = (pick(br, vL > vR) ? vL : vR) + cmax;
+  const S sL = (pick(br, fgt(vR, vL)) ? vL : vR) - cmax;
+  const S sR = (pick(br, fgt(vL, vR)) ? vL : vR) + cmax;
   const S rcL = WL[0] * (vL - sL);
   const S rcR = WR[0] * (sR - vR);
   const S den = rcR + rcL;
@@ -445,10 +459,10 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
     // swapped: one path with per-lane operands, so a warp whose lanes take
     // both sides (an FP64 warp instruction costs the same with any number of
     // active lanes) evaluates the reciprocal and quotients once
-    if (sL > 0.0) {
+    if (fgt(sL, 0.0)) {
       r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
-    } else if (vstar > 0.0 || sR > 0.0) {
-      const bool lft = vstar > 0.0;
+    } else if (fgt(vstar, 0.0) || fgt(sR, 0.0)) {
+      const bool lft = fgt(vstar, 0.0);
       const S s = lft ? sL : sR, v = lft ? vL : vR;
       const S w0 = lft ? WL[0] : WR[0], wP = lft ? WL[P_] : WR[P_], uP = lft ? UL[P_] : UR[P_];
       const S d = s - vstar;
@@ -459,15 +473,15 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
     } else {
       r = WR[0]; vg = vR; Pg = WR[P_]; e = UR[P_];
     }
-  } else if (pick(br, sL > 0.0)) {
+  } else if (pick(br, fgt(sL, 0.0))) {
     r = WL[0]; vg = vL; Pg = WL[P_]; e = UL[P_];
-  } else if (pick(br, vstar > 0.0)) {
+  } else if (pick(br, fgt(vstar, 0.0))) {
     const S d = sL - vstar;
     const S rd = recip_of(d);
     r = div_by(WL[0] * (sL - vL), d, rd);
     e = div_by((sL - vL) * UL[P_] - WL[P_] * vL + Pstar * vstar, d, rd);
     vg = vstar; Pg = Pstar;
-  } else if (pick(br, sR > 0.0)) {
+  } else if (pick(br, fgt(sR, 0.0))) {
     const S d = sR - vstar;
     const S rd = recip_of(d);
     r = div_by(WR[0] * (sR - vR), d, rd);
@@ -480,7 +494,7 @@ SPD_FN void hllc(const S* WL, const S* WR, const S* UL, const S* UR, S* F, doubl
   F[v1] = F[0] * vg + Pg;
   F[P_] = vg * (e + Pg);
   if (D > 1) {
-    const bool left = pick(br, vstar > 0.0);
+    const bool left = pick(br, fgt(vstar, 0.0));
 #pragma unroll
     for (int k = 1; k < D; ++k) {
       const int v = rvel<D>(idim, k);
