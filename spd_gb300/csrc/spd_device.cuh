@@ -266,6 +266,14 @@ SPD_FN bool fgt(double a, double b) {
   return a > b;
 #endif
 }
+// a >= b with IEEE semantics, the same way
+SPD_FN bool fge(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return !nan_w(a) && !nan_w(b) && ieee_key(__double_as_longlong(a)) >= ieee_key(__double_as_longlong(b));
+#else
+  return a >= b;
+#endif
+}
 template <int N> SPD_FN bool fgt(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
 template <int N> SPD_FN bool fgt(const Dual<N>& a, double b) { return a.v > b; }
 template <int N> SPD_FN bool fgt(double a, const Dual<N>& b) { return a > b.v; }
@@ -560,19 +568,20 @@ SPD_FN double dot_dir(const double* A, const double* x, int idim) {
 }
 
 // Limiters (src/muscl.py:12-59); NaN semantics follow the np.where forms.
+// (comparisons through fgt / fge: integer keys on the device)
 SPD_FN double minmod(double SL, double SR) {
   double r = SR / SL;
-  r = (r < 1.0) ? r : 1.0;
-  return ((r > 0.0) ? r : 0.0) * SL;
+  r = fgt(1.0, r) ? r : 1.0;
+  return (fgt(r, 0.0) ? r : 0.0) * SL;
 }
 SPD_FN double np_sign(double x) {
-  return (x > 0.0) ? 1.0 : ((x < 0.0) ? -1.0 : ((x == 0.0) ? 0.0 : x));
+  return fgt(x, 0.0) ? 1.0 : (fgt(0.0, x) ? -1.0 : ((fge(x, 0.0) && fge(0.0, x)) ? 0.0 : x));
 }
 SPD_FN double moncen(double dUL, double dUR, double dxL, double dxR, double dxM) {
   const double dUC = (dxL * dUL + dxR * dUR) / (dxL + dxR);
   double slope = np_min(abs_bits(2.0 * dUL * dxL / dxM), abs_bits(2.0 * dUR * dxR / dxM));
   slope = np_sign(dUC) * np_min(slope, abs_bits(dUC));
-  return (dUL * dUR >= 0.0) ? slope : 0.0;
+  return fge(dUL * dUR, 0.0) ? slope : 0.0;
 }
 
 // Limited slope with its branch as a decision code (BM as in Br): minmod

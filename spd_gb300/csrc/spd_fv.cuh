@@ -362,19 +362,20 @@ __device__ __forceinline__ double sed_alpha_dir(const double* W, long long e0, l
     const double rdv = 1.0 / dv;
     const double vL = dUm - dU0;
     const double vR = dUp - dU0;
-    const double selL = (dv < 0) ? ((vL > 0) ? vL : 0.0) : ((vL < 0) ? vL : 0.0);
+    // comparisons on the integer keys / words (IEEE semantics)
+    const double selL = fgt(0.0, dv) ? (fgt(vL, 0.0) ? vL : 0.0) : (fgt(0.0, vL) ? vL : 0.0);
     aL = div_rcp(-selL, dv, rdv);
-    if (abs_bits(dv) <= 0.0) aL = 1.0;
-    aL = (aL < 1.0) ? aL : 1.0;
-    const double selR = (dv > 0) ? ((vR > 0) ? vR : 0.0) : ((vR < 0) ? vR : 0.0);
+    if (!nonzero_w(dv)) aL = 1.0;  // |dv| <= 0
+    aL = fgt(1.0, aL) ? aL : 1.0;
+    const double selR = fgt(dv, 0.0) ? (fgt(vR, 0.0) ? vR : 0.0) : (fgt(0.0, vR) ? vR : 0.0);
     aR = div_rcp(selR, dv, rdv);
-    if (abs_bits(dv) <= 0.0) aR = 1.0;
-    aR = (aR < 1.0) ? aR : 1.0;
+    if (!nonzero_w(dv)) aR = 1.0;
+    aR = fgt(1.0, aR) ? aR : 1.0;
   };
   auto A = [&](int kk) {
     double aL, aR;
     aLR(kk, aL, aR);
-    return (aR < aL) ? aR : aL;
+    return fgt(aL, aR) ? aR : aL;
   };
   if (i == 0) return np_min(A(k), A(k + 1));
   if (i == Xd - 1) {
@@ -445,7 +446,8 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double 
   const long long e = ext_of<D>(g, ix, iy, iz);
   const unsigned m = mask[q];
   const int pt0 = m & 1u, ptP = (m >> P_) & 1u;
-  double t = (pt0 > ptP) ? (double)pt0 : (double)ptP;
+  // max(pt0, ptP) as a double: constants, no conversion on the FP64 pipe
+  double t = (pt0 | ptP) ? 1.0 : 0.0;
   if (pad) {
     double r = ext_new[e];
     double P = ext_new[(long long)P_ * g.Nqe + e];
@@ -454,9 +456,10 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, int pad, double 
       r = r + Weq[q];
       P = P + Weq[(long long)P_ * g.Nq + q];
     }
-    t = (r >= min_rho) ? t : 1.0;
-    t = (r <= max_rho) ? t : 1.0;
-    t = (P >= min_P) ? t : 1.0;
+    // comparisons on the integer keys (IEEE semantics: NaN fails them)
+    t = fge(r, min_rho) ? t : 1.0;
+    t = fge(max_rho, r) ? t : 1.0;
+    t = fge(P, min_P) ? t : 1.0;
   }
   theta_src[e] = t;
   troubles[q] = t;
