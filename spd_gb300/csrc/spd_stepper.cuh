@@ -21,12 +21,13 @@ static __device__ __forceinline__ void run(Blk B, const Geo& g, const double* __
     double c = sound_speed(W_cv[(long long)P_ * g.Nq + q], W_cv[q], g.gamma, g.min_c2) * (double)D;
 #pragma unroll
     for (int v = 1; v <= D; ++v) c = c + abs_bits(W_cv[(long long)v * g.Nq + q]);
-    if (c != c) isnan_c = true;
+    if (nan_w(c)) isnan_c = true;
     else cval = c;
   }
+  // the warp's maximum (comparisons on the integer keys)
   for (int off = 16; off > 0; off >>= 1) {
     const double o = __shfl_down_sync(0xffffffffu, cval, off);
-    cval = (o > cval) ? o : cval;
+    cval = fgt(o, cval) ? o : cval;
   }
   const unsigned nb = __ballot_sync(0xffffffffu, isnan_c);
   if ((threadIdx.x & 31) == 0) {
