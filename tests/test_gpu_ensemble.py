@@ -218,3 +218,33 @@ def test_packed_ensemble_with_viscosity_matches_individual_runs():
         assert a.time == b.time
         assert np.array_equal(a.dm.U_sp, b.dm.U_sp)
     ens.close()
+
+
+@pytest.mark.parametrize("kind", ["wb_potential", "isothermal"])
+def test_packed_ensemble_with_optional_physics_matches_individual_runs(kind):
+    """Well-balanced gravity columns (FV with limiting, "eq" boundaries,
+    equilibrium arrays per instance) and isothermal shear layers in packed
+    ensembles of uneven sides: each instance bit-identical to stepping it
+    alone."""
+    from spd_gb300 import SDADER_Ensemble, SDADER_Simulator
+    from spd_gb300 import initial_conditions as ics
+
+    def make(n, seed):
+        if kind == "wb_potential":
+            eq = ics.gravity_column(amp=0.0)
+            return SDADER_Simulator(p=2, N=(n, n), init_fct=ics.gravity_column(amp=0.05, step=True), eq_fct=eq,
+                                    WB=True, potential=True, update="FV", FB=True, riemann_solver_sd="hllc",
+                                    riemann_solver_fv="hllc", BC=(("periodic", "periodic"), ("eq", "eq")),
+                                    verbose=False)
+        return SDADER_Simulator(p=3, N=(n, n), init_fct=ics.kelvin_helmholtz(n, seed=seed), isothermal=True,
+                                update="FV", FB=True, riemann_solver_sd="hllc", riemann_solver_fv="hllc",
+                                BC=(("periodic", "periodic"),) * 2, verbose=False)
+
+    sides = [8, 12, 16]
+    ens_sims = [make(n, i) for i, n in enumerate(sides)]
+    solo = [make(n, i) for i, n in enumerate(sides)]
+    ens = SDADER_Ensemble(ens_sims, packed=True)
+    ens.perform_iterations(3)
+    _solo_steps(solo, 3)
+    _assert_same(ens_sims, solo, 3)
+    ens.close()
