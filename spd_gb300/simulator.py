@@ -450,8 +450,14 @@ class SD_Simulator(Simulator):
         Uploaded to the device (``upload_equilibrium``)."""
         p, n, ndim = self.p, self.p + 1, self.ndim
         W_gh = self.array_sp(ngh=self.Nghe)
+        # the quadrature points once for all variables; large grids build
+        # them and sum each variable on host thread slabs (bit-identical)
+        ncells = int(np.prod(W_gh.shape[1:ndim + 1]))
+        workers = min(16, os.cpu_count() or 1) if ncells >= (1 << 15) else 1
+        points = quadrature_points_threaded(self.mesh_cv, ndim, workers=workers)
         for var in range(self.nvar):
-            W_gh[var] = quadrature_mean(self.mesh_cv, self.eq_fct, ndim, var)
+            W_gh[var] = quadrature_mean(self.mesh_cv, self.eq_fct, ndim, var, points=points, workers=workers)
+        del points
         W_sp = self.compute_sp_from_cv(W_gh)
         U_sp = self.compute_conservatives(W_sp)
         eq = {"U_eq_sp": self.crop(U_sp)}
