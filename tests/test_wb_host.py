@@ -73,3 +73,24 @@ def test_eq_fv_fb_is_refused_only_without_wb(monkeypatch):
     kw.pop("eq_fct", None)
     with pytest.raises(NotImplementedError, match="WB=False"):
         build_host_only(monkeypatch, kw, meta, data)
+
+
+def test_threaded_equilibrium_sampling_is_bitwise(monkeypatch):
+    """Grids of more than 2^15 elements (ghosts included) sample the
+    equilibrium on host thread slabs: the arrays equal the one-thread ones
+    bit for bit."""
+    import os
+    from spd_gb300 import initial_conditions as ics
+    eq = ics.gravity_column(amp=0.0)
+    kw = dict(p=1, N=(182, 182), eq_fct=eq, WB=True, potential=True, update="FV", FB=True,
+              BC=(("periodic", "periodic"), ("eq", "eq")))
+    monkeypatch.setattr(sim_mod.SD_Simulator, "_create_context", lambda self: setattr(self, "_ctx", FakeContext()))
+    monkeypatch.setattr(sim_mod.SD_Simulator, "compute_dt", lambda self: None)
+    monkeypatch.setattr(os, "cpu_count", lambda: 4)
+    many = sim_mod.SDADER_Simulator(init_fct=eq, verbose=False, **kw)._ctx.uploads
+    monkeypatch.setattr(os, "cpu_count", lambda: 1)
+    one = sim_mod.SDADER_Simulator(init_fct=eq, verbose=False, **kw)._ctx.uploads
+    names = [k for k in many if "_eq_" in k]
+    assert len(names) == 2 + 2 * 2 + 2 * 2 + 1
+    for k in names:
+        assert np.array_equal(many[k], one[k]), k
